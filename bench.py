@@ -1,0 +1,320 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 Black-Scholes map (options/s and % HBM roofline).
+
+Default workload (the headline): the plain map over 10,000,000 seeded options
+(S~U[10,200], K=S*U[0.5,1.5], r~U[0.01,0.10], v~U[0.05,0.65], t~U[0.05,2],
+calls/puts 50/50), FP32, NUM_RUNS = 100 passes per step -- one step is one
+whole ROI of the reference benchmark (blackscholes.c:781-913).  The 280 MB
+working set is larger than the 129 MB L2, so every pass streams from HBM.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--config map|batch|precision|serve]
+
+One JSON line on stdout (rank 0).  Under torchrun each rank prices its own
+book on its own GPU (weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_OPTIONS = 10_000_000
+NUM_RUNS = 100
+BYTES_PER_OPTION = 28  # 5 float inputs + int32 otype + float price
+METRIC = "options/sec & %HBM roofline"
+UNIT = "options/s"
+SEED = 20241203
+# DRAM bytes per option per pass of the fast map kernel, from the ncu capture
+# summarised in profiles/ (dram__bytes_read.sum + dram__bytes_write.sum of one
+# launch / options in that launch).  None until captured.
+NCU_DRAM_BYTES_PER_OPTION = None
+NCU_PROFILE = "profiles/map_fast_10M.md"
+
+
+# ------------------------------------------------------------------ ranks
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def shard_range(n: int, rank: int, world: int):
+    """Contiguous (offset, len) of rank's share of n independent options
+    (the same rule as the reference's static partition)."""
+    q, r = divmod(n, world)
+    off = rank * q + min(rank, r)
+    return off, q + (1 if rank < r else 0)
+
+
+def init_group(world: int, backend: str):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def barrier(dist, device=None):
+    if dist is not None:
+        if device is not None:
+            dist.barrier(device_ids=[device])
+        else:
+            dist.barrier()
+
+
+def reduce_max(dist, x: float, device=None) -> float:
+    """Max over ranks (timing only; the data path has no collective)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64,
+                     device=f"cuda:{device}" if device is not None else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------- clocks
+CLOCK_QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+class ClockSampler:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={CLOCK_QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def measured_hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# -------------------------------------------------------------- CPU baseline
+def cpu_baseline(book, target_s: float = 10.0):
+    """The oracle port of the reference's FastFlow map on every host core,
+    over the same book, with as many passes as fit in ~target_s seconds."""
+    import oracle
+    threads = os.cpu_count() or 1
+    _, t1 = oracle.bs_map(book, threads, 1)
+    runs = int(max(1, min(NUM_RUNS, target_s / max(t1, 1e-6))))
+    _, secs = oracle.bs_map(book, threads, runs)
+    return {"value": len(book) * runs / secs, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(book)} options x {runs} passes (of {NUM_RUNS}) of the same book, "
+                      f"static partition over {threads} threads, {secs:.2f} s"}
+
+
+# ------------------------------------------------------------------ our arm
+def run_ours(args, rank, world, local):
+    import torch
+
+    from p3arsec_gb300 import Context, books
+    from p3arsec_gb300 import build as b
+    os.environ.setdefault("BSG_TUNE_CACHE", os.path.join(b.BUILD, "tune_cache.txt"))
+    b.build()
+    torch.cuda.set_device(local)
+    dist = init_group(world, "nccl")
+    n, runs = args.n, args.runs
+    book = books.generate(n, seed=SEED + rank)
+    ctx = Context(local, max_options=n)
+    tune = ctx.autotune(n)
+    dev = [torch.from_numpy(a).to(f"cuda:{local}") for a in book.arrays()]
+    out = torch.empty(n, dtype=torch.float32, device=f"cuda:{local}")
+    stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{local}")
+
+    def step():
+        ctx.price_soa(*dev, out, n=n, num_runs=runs, device=True, asynchronous=True)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(dist, local)
+    torch.cuda.synchronize()
+    l0 = ctx.launches
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        e1.synchronize()
+    torch.cuda.synchronize()
+    launches = ctx.launches - l0
+    ms = e0.elapsed_time(e1)
+    barrier(dist, local)
+    ms_max = reduce_max(dist, ms, local)
+    secs = ms_max / 1e3
+    value = world * n * runs * args.steps / secs
+    per_launch_s = secs / (runs * args.steps)
+    achieved = BYTES_PER_OPTION * n / per_launch_s / 1e9
+    peak, peak_src = measured_hbm_peak()
+
+    # accuracy of the timed output against the FP64 oracle kernel
+    edges = np.array([0.0, 0.5, 1.0, 2.0, 3.0, 4.0, 6.0, np.inf])
+    rep = ctx.error_report(dev, out, n, edges)
+    max_abs = max(x["max_abs"] for x in rep)
+    rms = (sum(x["sum_sq_abs"] for x in rep) / n) ** 0.5
+
+    # end to end through the public API with pinned host buffers
+    host = [torch.from_numpy(a).pin_memory().numpy() for a in book.arrays()]
+    hout = torch.empty(n, dtype=torch.float32).pin_memory().numpy()
+    ctx.price_soa(*host, hout, n=n, num_runs=runs)  # warm (graph for the resident buffers)
+    barrier(dist, local)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.price_soa(*host, hout, n=n, num_runs=runs)
+    e2e_s = reduce_max(dist, time.perf_counter() - t0, local)
+    e2e = {"value": world * n * runs * args.steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 4 * n,
+           "ms_per_step": 1e3 * e2e_s / args.steps}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded book, reference config distributions)",
+        "config": {"workload": f"plain map, {n} European options FP32 SoA, NUM_RUNS={runs} "
+                               "passes per step", "options": n, "num_runs": runs,
+                   "parallelism": f"replicas x{world} (independent books)",
+                   "l2": "inputs (280 MB) larger than L2 (129 MB); no flush",
+                   "tune": tune, "mode": "fast"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_src,
+                     "traffic": (NCU_DRAM_BYTES_PER_OPTION * n
+                                 if NCU_DRAM_BYTES_PER_OPTION else None),
+                     "traffic_source": NCU_PROFILE if NCU_DRAM_BYTES_PER_OPTION else None,
+                     "bytes_per_launch": BYTES_PER_OPTION * n,
+                     "avg_launch_us": per_launch_s * 1e6},
+        "accuracy": {"max_abs_vs_fp64": max_abs, "rms_abs_vs_fp64": rms, "gate": 1e-4},
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(book)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+# ---------------------------------------------------------- reference arm
+def run_reference(args, rank, world, local):
+    """The reference's CPU path (the oracle port of its FastFlow map: same
+    arithmetic bit for bit, static partition, a join per pass) on every host
+    core.  Rank 0 only; other ranks exit without work."""
+    if rank != 0:
+        return
+    import oracle
+    from p3arsec_gb300 import books
+    oracle.build(ref=False)
+    n = args.n
+    book = books.generate(n, seed=SEED)
+    threads = os.cpu_count() or 1
+    _, t1 = oracle.bs_map(book, threads, 1)
+    runs = int(max(1, min(args.runs, round(2.0 / max(t1, 1e-6)))))
+    for _ in range(args.warmup):
+        oracle.bs_map(book, threads, runs)
+    total = 0.0
+    for _ in range(args.steps):
+        _, s = oracle.bs_map(book, threads, runs)
+        total += s
+    value = n * runs * args.steps / total
+    sample = (f"each step {n} options x {runs} passes (of {NUM_RUNS}) on {threads} threads")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded book, reference config distributions)",
+        "config": {"workload": f"plain map, {n} European options FP32 SoA, NUM_RUNS={args.runs} "
+                               "passes per step", "options": n, "num_runs": args.runs},
+        "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", choices=["map"], default="map")
+    ap.add_argument("--n", type=int, default=N_OPTIONS)
+    ap.add_argument("--runs", type=int, default=NUM_RUNS)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world, local)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

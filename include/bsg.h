@@ -1,0 +1,175 @@
+/*
+ * bsg.h -- C ABI of libbsgpu.so, the GB300 (sm_103a) Black-Scholes map.
+ *
+ * Replaces the hot path of P3ARSEC's blackscholes benchmark
+ * (parsec-ff/pkgs/apps/blackscholes/src/blackscholes.c): BlkSchlsEqEuroNoDiv
+ * and its polynomial CNDF applied to SoA option arrays NUM_RUNS times.
+ *
+ * Conventions (the reference's, plus status codes):
+ *  - The caller owns every buffer.  Arrays are the reference's SoA layout
+ *    (blackscholes.c:103-113, 747-767): five float arrays sptprice, strike,
+ *    rate, volatility, otime; int32 otype (1 = put, 0 = call); float prices.
+ *  - Every call returns a bsg_status (0 = ok, < 0 = error) instead of
+ *    printing and calling exit() as the reference does (blackscholes.c:697-739).
+ *    bsg_last_error() gives a message for the last failure on a context.
+ *  - A context owns one device, one stream, resident device buffers for up
+ *    to max_options options, cached CUDA graphs and the tuning choice.  Calls
+ *    on one context are serialised by a lock; use one context per host
+ *    thread for concurrency.
+ *  - No call ever falls back to a CPU computation: without a usable GPU,
+ *    bsg_create fails with BSG_ERR_NO_DEVICE.
+ */
+#ifndef BSG_H
+#define BSG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BSG_ABI_VERSION 1
+
+typedef struct bsg_ctx bsg_ctx;
+
+typedef enum bsg_status {
+    BSG_OK = 0,
+    BSG_ERR_INVALID_ARG = -1,   /* null pointer, negative count, bad flag */
+    BSG_ERR_NO_DEVICE = -2,     /* no CUDA device / bad ordinal / not sm_103 */
+    BSG_ERR_CUDA = -3,          /* a CUDA runtime call failed */
+    BSG_ERR_OUT_OF_MEMORY = -4, /* device or pinned host allocation failed */
+    BSG_ERR_CAPACITY = -5,      /* n exceeds the context's max_options */
+    BSG_ERR_MISALIGNED = -6,    /* device pointer not 4-byte aligned */
+    BSG_ERR_TIMEOUT = -7,       /* a bounded wait expired */
+    BSG_ERR_BUDGET = -8,        /* request larger than the admission budget */
+    BSG_ERR_CANCELLED = -9,     /* request cancelled while queued */
+    BSG_ERR_NOT_SUPPORTED = -10,
+    BSG_ERR_STATE = -11         /* call not valid in the object's state */
+} bsg_status;
+
+/* ---- flags ------------------------------------------------------------ */
+#define BSG_HOST_PTRS     0x000u /* host arrays: copied in and out inside the call */
+#define BSG_DEVICE_PTRS   0x001u /* device arrays on the context's device */
+#define BSG_ASYNC         0x002u /* device pointers only: return once enqueued */
+#define BSG_MODE_FAST     0x000u /* compensated FP32 with SFU approximations */
+#define BSG_MODE_SFU_REF  0x010u /* reference operation order, SFU approximations */
+#define BSG_MODE_LIBM_REF 0x020u /* reference operation order, accurate libm / IEEE */
+#define BSG_MODE_MASK     0x0F0u
+#define BSG_NO_GRAPH      0x100u /* launch NUM_RUNS kernels directly, no graph */
+
+#define BSG_NUM_RUNS 100 /* blackscholes.c:87 */
+
+/* ---- context ---------------------------------------------------------- */
+
+/* New context on CUDA device `device` able to price up to max_options per
+ * call with host pointers (device-pointer calls have no size limit).
+ * Allocates 28 * max_options bytes of device memory. */
+int bsg_create(bsg_ctx** out, int device, size_t max_options);
+void bsg_destroy(bsg_ctx* ctx);
+const char* bsg_strerror(int status);
+const char* bsg_last_error(const bsg_ctx* ctx);
+/* The context's cudaStream_t (as void*): work of every call is ordered on it. */
+void* bsg_stream(bsg_ctx* ctx);
+/* Number of kernels this context has launched so far. */
+uint64_t bsg_kernel_launches(const bsg_ctx* ctx);
+
+/* Pinned host memory for staging (cudaMallocHost); NULL on failure. */
+void* bsg_host_alloc(size_t bytes);
+void bsg_host_free(void* p);
+
+/* ---- the map -----------------------------------------------------------
+ * prices[i] = BlkSchlsEqEuroNoDiv(sptprice[i], strike[i], rate[i],
+ *             volatility[i], otime[i], otype[i]) for i < n, evaluated
+ * num_runs times (each run a full pass over the n options, as the
+ * reference's NUM_RUNS loop, blackscholes.c:315-348 / 607-658).
+ * Replaces bs_thread (blackscholes.c:607) and the FastFlow map's svc
+ * (blackscholes.c:316-346).  n == 0 or num_runs == 0 is a no-op. */
+int bsg_price_soa(bsg_ctx* ctx, const float* sptprice, const float* strike,
+                  const float* rate, const float* volatility,
+                  const float* otime, const int32_t* otype, float* prices,
+                  size_t n, int num_runs, unsigned flags);
+
+/* The reference's batch signature (blackscholes.simd.c:221-223): one pass
+ * over numOptions options on the default context of device 0, host
+ * pointers.  timet is unused, as in the reference. */
+int bsg_BlkSchlsEqEuroNoDiv(float* OptionPrice, int numOptions, float* sptprice,
+                            float* strike, float* rate, float* volatility,
+                            float* time, int* otype, float timet);
+
+/* FP64 evaluation of the same formula (validation oracle kernel).  Same
+ * pointer rules as bsg_price_soa; out is double. */
+int bsg_price_fp64(bsg_ctx* ctx, const float* sptprice, const float* strike,
+                   const float* rate, const float* volatility,
+                   const float* otime, const int32_t* otype, double* out,
+                   size_t n, unsigned flags);
+
+/* ---- batched books -----------------------------------------------------
+ * Many independent books stored in one SoA pool of pool_len options; book b
+ * occupies [segs[b].offset, segs[b].offset + segs[b].len).  One persistent
+ * kernel prices every book (tiles handed out by a device work counter), and
+ * num_runs passes are replayed from a captured CUDA graph.  Pool pointers
+ * are device pointers; segs is a host array.  Segments must lie inside the
+ * pool; they may be in any order but must not overlap. */
+typedef struct bsg_segment {
+    uint64_t offset;
+    uint64_t len;
+} bsg_segment;
+
+int bsg_price_batch(bsg_ctx* ctx, const float* sptprice, const float* strike,
+                    const float* rate, const float* volatility,
+                    const float* otime, const int32_t* otype, float* prices,
+                    size_t pool_len, const bsg_segment* segs, size_t nseg,
+                    int num_runs, unsigned flags);
+
+/* The same books priced by one plain map launch per book (the comparison
+ * baseline for bsg_price_batch). */
+int bsg_price_books_plain(bsg_ctx* ctx, const float* sptprice, const float* strike,
+                          const float* rate, const float* volatility,
+                          const float* otime, const int32_t* otype, float* prices,
+                          size_t pool_len, const bsg_segment* segs, size_t nseg,
+                          int num_runs, unsigned flags);
+
+/* ---- accuracy report ---------------------------------------------------
+ * Compares FP32 prices (device) with the FP64 oracle evaluated on the same
+ * device inputs, bucketed by |d1| (FP64) against the ascending bucket edges
+ * edges[0..nbuckets] (an option with |d1| outside [edges[0], edges[nbuckets])
+ * lands in the first / last bucket).  Relative error uses |oracle| with a
+ * floor of rel_floor. */
+typedef struct bsg_err_bucket {
+    uint64_t count;
+    double max_abs;
+    double sum_sq_abs;
+    double max_rel;
+    double max_price;
+} bsg_err_bucket;
+
+#define BSG_MAX_ERR_BUCKETS 32
+
+int bsg_error_report(bsg_ctx* ctx, const float* sptprice, const float* strike,
+                     const float* rate, const float* volatility,
+                     const float* otime, const int32_t* otype,
+                     const float* prices, size_t n, const double* edges,
+                     int nbuckets, double rel_floor, bsg_err_bucket* out);
+
+/* ---- tuning ------------------------------------------------------------
+ * The plain map is a family of kernels: vector width per thread, block size
+ * and grid size.  bsg_autotune times the candidates on the context's device
+ * for n options and makes the fastest the context's choice; the result is
+ * cached in the file named by $BSG_TUNE_CACHE (if set) per (device, size
+ * bucket). */
+typedef struct bsg_tune {
+    int vec_per_thread; /* float4 groups per thread per tile: 1, 2 or 4 */
+    int block;          /* threads per block: 128, 256 or 512 */
+    int blocks_per_sm;  /* grid = blocks_per_sm * SM count; 0 = one block per tile */
+    int load_path;      /* 0 = LDG.128 non-coherent, 1 = LDG.128 evict-first */
+} bsg_tune;
+
+int bsg_autotune(bsg_ctx* ctx, size_t n, bsg_tune* out);
+int bsg_get_tune(const bsg_ctx* ctx, bsg_tune* out);
+int bsg_set_tune(bsg_ctx* ctx, const bsg_tune* tune);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BSG_H */

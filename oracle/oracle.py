@@ -1,0 +1,142 @@
+"""ctypes wrappers of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+* ``libbsoracle.so`` -- the C restatement of the reference's pricing path
+  (bs_oracle.c; blackscholes.c:126-258 and the FastFlow map driver
+  blackscholes.c:315-348), plus the FP64 same-formula oracle.  Built here and
+  on any machine with gcc.
+* ``_ref/libbsref.so`` -- the reference's own blackscholes.c compiled from its
+  source tree (only where that tree is present).
+
+The FP32 restatement is bit-identical to the reference on the same inputs
+(pinned by tests/golden against outputs of the compiled reference).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "libbsoracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libbsref.so")
+REF_SRC = os.path.join("/root/reference", "parsec-ff", "pkgs", "apps", "blackscholes",
+                       "src", "blackscholes.c")
+
+_P = ctypes.c_void_p
+_lib = None
+_ref = None
+
+
+def build(ref: bool = True) -> None:
+    """make the restatement; and the reference (when its source tree exists)."""
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    if ref and os.path.exists(REF_SRC):
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO) or (
+                os.path.getmtime(ORACLE_SO) < os.path.getmtime(os.path.join(HERE, "bs_oracle.c"))):
+            build(ref=False)
+        L = ctypes.CDLL(ORACLE_SO)
+        L.bso_cndf_ref.restype = ctypes.c_float
+        L.bso_cndf_ref.argtypes = [ctypes.c_float]
+        L.bso_price_ref.restype = ctypes.c_float
+        L.bso_price_ref.argtypes = [ctypes.c_float] * 5 + [ctypes.c_int]
+        L.bso_cndf_fp64.restype = ctypes.c_double
+        L.bso_cndf_fp64.argtypes = [ctypes.c_double]
+        L.bso_price_fp64.restype = ctypes.c_double
+        L.bso_price_fp64.argtypes = [ctypes.c_double] * 5 + [ctypes.c_int]
+        L.bso_d1_fp64.restype = ctypes.c_double
+        L.bso_d1_fp64.argtypes = [ctypes.c_double] * 5
+        L.bso_price_ref_soa.restype = None
+        L.bso_price_ref_soa.argtypes = [ctypes.c_size_t] + [_P] * 7
+        L.bso_price_fp64_soa.restype = None
+        L.bso_price_fp64_soa.argtypes = [ctypes.c_size_t] + [_P] * 7
+        L.bso_static_partition.restype = None
+        L.bso_static_partition.argtypes = [ctypes.c_int64, ctypes.c_int, _P, _P]
+        L.bso_bs_map.restype = ctypes.c_double
+        L.bso_bs_map.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_size_t] + [_P] * 7
+        _lib = L
+    return _lib
+
+
+def ref_lib():
+    """The compiled reference (None where its source tree was absent)."""
+    global _ref
+    if _ref is None and os.path.exists(REF_SO):
+        R = ctypes.CDLL(REF_SO)
+        R.bsref_price_soa.restype = None
+        R.bsref_price_soa.argtypes = [ctypes.c_size_t] + [_P] * 7
+        R.bsref_cndf.restype = None
+        R.bsref_cndf.argtypes = [ctypes.c_size_t, _P, _P]
+        _ref = R
+    return _ref
+
+
+def _arrs(book):
+    arrs = [np.ascontiguousarray(a, dtype=np.float32) for a in book.arrays()[:5]]
+    arrs.append(np.ascontiguousarray(book.otype, dtype=np.int32))
+    return arrs
+
+
+def _p(a):
+    return a.ctypes.data_as(_P)
+
+
+def price_ref(book) -> np.ndarray:
+    """FP32 restatement (bit-identical to the reference)."""
+    a = _arrs(book)
+    out = np.empty(len(book), dtype=np.float32)
+    lib().bso_price_ref_soa(len(book), *[_p(x) for x in a], _p(out))
+    return out
+
+
+def price_fp64(book) -> np.ndarray:
+    """FP64 evaluation of the same formula on the float32 inputs."""
+    a = _arrs(book)
+    out = np.empty(len(book), dtype=np.float64)
+    lib().bso_price_fp64_soa(len(book), *[_p(x) for x in a], _p(out))
+    return out
+
+
+def d1_fp64(book) -> np.ndarray:
+    s, k, r, v, t = (np.asarray(x, dtype=np.float64) for x in book.arrays()[:5])
+    return ((r + v * v * 0.5) * t + np.log(s / k)) / (v * np.sqrt(t))
+
+
+def price_reference(book):
+    """The compiled reference's own BlkSchlsEqEuroNoDiv (None if not built)."""
+    R = ref_lib()
+    if R is None:
+        return None
+    a = _arrs(book)
+    out = np.empty(len(book), dtype=np.float32)
+    R.bsref_price_soa(len(book), *[_p(x) for x in a], _p(out))
+    return out
+
+
+def cndf_ref(x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    return np.array([lib().bso_cndf_ref(float(v)) for v in x], dtype=np.float32)
+
+
+def static_partition(n: int, nw: int):
+    b = np.empty(nw, dtype=np.int64)
+    e = np.empty(nw, dtype=np.int64)
+    lib().bso_static_partition(n, nw, _p(b), _p(e))
+    return b, e
+
+
+def bs_map(book, nthreads: int, num_runs: int):
+    """The threaded NUM_RUNS map driver; returns (prices, roi_seconds)."""
+    a = _arrs(book)
+    out = np.empty(len(book), dtype=np.float32)
+    secs = lib().bso_bs_map(nthreads, num_runs, len(book), *[_p(x) for x in a], _p(out))
+    if secs < 0:
+        raise RuntimeError("bso_bs_map failed")
+    return out, secs

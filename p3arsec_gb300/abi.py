@@ -1,0 +1,269 @@
+"""ctypes binding of libbsgpu.so (the C ABI declared in include/bsg.h).
+
+This module is the Python side of the drop-in boundary: it loads the
+in-tree library and fails loudly when it is missing -- there is no CPU
+fallback.  Pointer arguments accept numpy arrays (host), objects with a
+``data_ptr()`` method such as torch CUDA tensors (device), or raw ints.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libbsgpu.so")
+
+# flags (include/bsg.h)
+HOST_PTRS = 0x000
+DEVICE_PTRS = 0x001
+ASYNC = 0x002
+MODE_FAST = 0x000
+MODE_SFU_REF = 0x010
+MODE_LIBM_REF = 0x020
+NO_GRAPH = 0x100
+NUM_RUNS = 100
+MAX_ERR_BUCKETS = 32
+
+MODES = {"fast": MODE_FAST, "sfu_ref": MODE_SFU_REF, "libm_ref": MODE_LIBM_REF}
+
+STATUS = {
+    0: "BSG_OK", -1: "BSG_ERR_INVALID_ARG", -2: "BSG_ERR_NO_DEVICE",
+    -3: "BSG_ERR_CUDA", -4: "BSG_ERR_OUT_OF_MEMORY", -5: "BSG_ERR_CAPACITY",
+    -6: "BSG_ERR_MISALIGNED", -7: "BSG_ERR_TIMEOUT", -8: "BSG_ERR_BUDGET",
+    -9: "BSG_ERR_CANCELLED", -10: "BSG_ERR_NOT_SUPPORTED", -11: "BSG_ERR_STATE",
+}
+
+
+class BsgError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        self.status = status
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+
+
+class Segment(ctypes.Structure):
+    _fields_ = [("offset", ctypes.c_uint64), ("len", ctypes.c_uint64)]
+
+
+class ErrBucket(ctypes.Structure):
+    _fields_ = [("count", ctypes.c_uint64), ("max_abs", ctypes.c_double),
+                ("sum_sq_abs", ctypes.c_double), ("max_rel", ctypes.c_double),
+                ("max_price", ctypes.c_double)]
+
+
+class Tune(ctypes.Structure):
+    _fields_ = [("vec_per_thread", ctypes.c_int), ("block", ctypes.c_int),
+                ("blocks_per_sm", ctypes.c_int), ("load_path", ctypes.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+# Every symbol the header declares, with its ctypes signature.
+_P = ctypes.c_void_p
+_SZ = ctypes.c_size_t
+_I = ctypes.c_int
+_U = ctypes.c_uint
+SIGNATURES = {
+    "bsg_create": (_I, [ctypes.POINTER(_P), _I, _SZ]),
+    "bsg_destroy": (None, [_P]),
+    "bsg_strerror": (ctypes.c_char_p, [_I]),
+    "bsg_last_error": (ctypes.c_char_p, [_P]),
+    "bsg_stream": (_P, [_P]),
+    "bsg_kernel_launches": (ctypes.c_uint64, [_P]),
+    "bsg_host_alloc": (_P, [_SZ]),
+    "bsg_host_free": (None, [_P]),
+    "bsg_price_soa": (_I, [_P] + [_P] * 7 + [_SZ, _I, _U]),
+    "bsg_BlkSchlsEqEuroNoDiv": (_I, [_P, _I] + [_P] * 6 + [ctypes.c_float]),
+    "bsg_price_fp64": (_I, [_P] + [_P] * 7 + [_SZ, _U]),
+    "bsg_price_batch": (_I, [_P] + [_P] * 7 + [_SZ, ctypes.POINTER(Segment), _SZ, _I, _U]),
+    "bsg_price_books_plain": (_I, [_P] + [_P] * 7 + [_SZ, ctypes.POINTER(Segment), _SZ, _I, _U]),
+    "bsg_error_report": (_I, [_P] + [_P] * 7 + [_SZ, _P, _I, ctypes.c_double, ctypes.POINTER(ErrBucket)]),
+    "bsg_autotune": (_I, [_P, _SZ, ctypes.POINTER(Tune)]),
+    "bsg_get_tune": (_I, [_P, ctypes.POINTER(Tune)]),
+    "bsg_set_tune": (_I, [_P, ctypes.POINTER(Tune)]),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Load libbsgpu.so (once).  Raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{path} is missing: build the CUDA library first "
+            "(python -m p3arsec_gb300.build); there is no CPU fallback")
+    lib = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def ptr(x) -> int:
+    """Address of a numpy array, a tensor-like with data_ptr(), or an int."""
+    if x is None:
+        return 0
+    if isinstance(x, int):
+        return x
+    if isinstance(x, np.ndarray):
+        return x.ctypes.data
+    if hasattr(x, "data_ptr"):
+        return int(x.data_ptr())
+    raise TypeError(f"cannot take the address of {type(x)!r}")
+
+
+def _check(lib, ctx, st):
+    if st != 0:
+        msg = lib.bsg_last_error(ctx).decode() if ctx else ""
+        if not msg:
+            msg = lib.bsg_strerror(st).decode()
+        raise BsgError(st, msg)
+
+
+class Context:
+    """One GPU pricing context (bsg_ctx): a device, a stream, resident buffers."""
+
+    def __init__(self, device: int = 0, max_options: int = 1 << 20):
+        self.lib = load()
+        h = _P()
+        st = self.lib.bsg_create(ctypes.byref(h), device, max_options)
+        if st != 0:
+            raise BsgError(st, self.lib.bsg_strerror(st).decode())
+        self.h = h
+        self.device = device
+        self.max_options = max_options
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.bsg_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.bsg_stream(self.h) or 0)
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.bsg_kernel_launches(self.h))
+
+    # ------------------------------------------------------------ pricing
+    def price_soa(self, s, k, r, v, t, otype, prices, n=None, num_runs=1,
+                  mode="fast", device=False, asynchronous=False, graph=True):
+        """bsg_price_soa over host numpy arrays or device pointers."""
+        if n is None:
+            n = len(s)
+        flags = MODES[mode] | (DEVICE_PTRS if device else HOST_PTRS)
+        if asynchronous:
+            flags |= ASYNC
+        if not graph:
+            flags |= NO_GRAPH
+        if not device:
+            for a, dt in ((s, np.float32), (k, np.float32), (r, np.float32), (v, np.float32),
+                          (t, np.float32), (otype, np.int32), (prices, np.float32)):
+                if not (isinstance(a, np.ndarray) and a.dtype == dt and a.flags.c_contiguous
+                        and a.shape[0] >= n):
+                    raise TypeError("host arrays must be C-contiguous float32 (otype int32) of length >= n")
+        st = self.lib.bsg_price_soa(self.h, ptr(s), ptr(k), ptr(r), ptr(v), ptr(t), ptr(otype),
+                                    ptr(prices), n, num_runs, flags)
+        _check(self.lib, self.h, st)
+        return prices
+
+    def price_book(self, book, num_runs=1, mode="fast"):
+        """Prices a host ``books.Book``; returns a new float32 array."""
+        out = np.empty(len(book), dtype=np.float32)
+        self.price_soa(*book.arrays(), out, n=len(book), num_runs=num_runs, mode=mode)
+        return out
+
+    def price_fp64(self, s, k, r, v, t, otype, out, n=None, device=False):
+        if n is None:
+            n = len(s)
+        flags = DEVICE_PTRS if device else HOST_PTRS
+        st = self.lib.bsg_price_fp64(self.h, ptr(s), ptr(k), ptr(r), ptr(v), ptr(t), ptr(otype),
+                                     ptr(out), n, flags)
+        _check(self.lib, self.h, st)
+        return out
+
+    def price_batch(self, pool, prices, pool_len, segments, num_runs=1, mode="fast",
+                    plain=False, asynchronous=False, graph=True):
+        """Batched books over a device pool (pool = 6 device pointers)."""
+        segs = (Segment * max(len(segments), 1))()
+        for i, (o, l) in enumerate(segments):
+            segs[i].offset = int(o)
+            segs[i].len = int(l)
+        flags = MODES[mode] | DEVICE_PTRS
+        if asynchronous:
+            flags |= ASYNC
+        if not graph:
+            flags |= NO_GRAPH
+        fn = self.lib.bsg_price_books_plain if plain else self.lib.bsg_price_batch
+        st = fn(self.h, *[ptr(x) for x in pool], ptr(prices), pool_len, segs, len(segments),
+                num_runs, flags)
+        _check(self.lib, self.h, st)
+
+    def error_report(self, pool, prices, n, edges, rel_floor=1e-3):
+        """bsg_error_report over device arrays; returns a list of dicts."""
+        edges = np.ascontiguousarray(edges, dtype=np.float64)
+        nb = len(edges) - 1
+        out = (ErrBucket * nb)()
+        st = self.lib.bsg_error_report(self.h, *[ptr(x) for x in pool], ptr(prices), n,
+                                       ptr(edges), nb, rel_floor, out)
+        _check(self.lib, self.h, st)
+        res = []
+        for i in range(nb):
+            b = out[i]
+            res.append({"d1_lo": float(edges[i]), "d1_hi": float(edges[i + 1]),
+                        "count": int(b.count), "max_abs": b.max_abs,
+                        "rms_abs": (b.sum_sq_abs / b.count) ** 0.5 if b.count else 0.0,
+                        "sum_sq_abs": b.sum_sq_abs, "max_rel": b.max_rel,
+                        "max_price": b.max_price})
+        return res
+
+    # ------------------------------------------------------------- tuning
+    def autotune(self, n: int) -> dict:
+        t = Tune()
+        st = self.lib.bsg_autotune(self.h, n, ctypes.byref(t))
+        _check(self.lib, self.h, st)
+        return t.as_dict()
+
+    def get_tune(self) -> dict:
+        t = Tune()
+        _check(self.lib, self.h, self.lib.bsg_get_tune(self.h, ctypes.byref(t)))
+        return t.as_dict()
+
+    def set_tune(self, vec_per_thread=1, block=256, blocks_per_sm=0, load_path=0):
+        t = Tune(vec_per_thread, block, blocks_per_sm, load_path)
+        _check(self.lib, self.h, self.lib.bsg_set_tune(self.h, ctypes.byref(t)))
+
+
+def BlkSchlsEqEuroNoDiv(OptionPrice, numOptions, sptprice, strike, rate, volatility,
+                        time, otype, timet=0.0):
+    """The reference's batch entry point (blackscholes.simd.c:221-223) on the GPU.
+
+    Prices ``numOptions`` options once into ``OptionPrice`` (host float32
+    arrays; otype int32).  ``timet`` is unused, as in the reference.
+    """
+    lib = load()
+    st = lib.bsg_BlkSchlsEqEuroNoDiv(ptr(OptionPrice), numOptions, ptr(sptprice), ptr(strike),
+                                     ptr(rate), ptr(volatility), ptr(time), ptr(otype), timet)
+    if st != 0:
+        raise BsgError(st, lib.bsg_strerror(st).decode())
+    return OptionPrice

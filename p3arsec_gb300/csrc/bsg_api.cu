@@ -1,0 +1,807 @@
+// bsg_api.cu -- the C ABI of libbsgpu.so (declared in include/bsg.h).
+//
+// A context owns a device, a stream, resident buffers for host-pointer calls,
+// a small cache of instantiated CUDA graphs (the NUM_RUNS loop replayed as
+// one graph launch), device scratch for batch segment tables and error
+// accumulators, and the tuning choice of the plain map.
+//
+// Safety: every device pointer handed in is checked against the extent of
+// the allocation that contains it (cuMemGetAddressRange) before any kernel
+// reads or writes through it, so a wrong size or pointer from the caller is
+// a status code, never an out-of-bounds access on the GPU.
+#include "bsg.h"
+#include "bsg_internal.h"
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <sstream>
+#include <string>
+#include <vector>
+
+namespace {
+
+constexpr size_t kGraphCacheSize = 8;
+
+struct GraphKey {
+    bsg::SoA soa;
+    int64_t n;
+    int runs;
+    int mode;
+    bsg::MapCfg cfg;
+    int kind;  // 0 plain map, 1 batch
+    uint64_t ntiles;
+    int nseg;
+    bool operator==(const GraphKey& o) const {
+        return std::memcmp(this, &o, sizeof(GraphKey)) == 0;
+    }
+};
+
+struct GraphEntry {
+    GraphKey key;
+    cudaGraphExec_t exec;
+};
+
+int mode_of(unsigned flags) {
+    switch (flags & BSG_MODE_MASK) {
+        case BSG_MODE_FAST: return bsg::MODE_FAST;
+        case BSG_MODE_SFU_REF: return bsg::MODE_SFU_REF;
+        case BSG_MODE_LIBM_REF: return bsg::MODE_LIBM_REF;
+        default: return -1;
+    }
+}
+
+size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace
+
+struct bsg_ctx {
+    int device = 0;
+    int sm_count = 0;
+    int batch_blocks_per_sm = 1;
+    cudaStream_t stream = nullptr;
+    size_t cap = 0;     // max_options
+    size_t cap_al = 0;  // per-array stride in the resident buffer
+    char* dev_buf = nullptr;
+    bsg::MapCfg tune{1, 256, 0, 0};
+    std::mutex mu;
+    std::string err;
+    uint64_t launches = 0;
+    std::vector<GraphEntry> graphs;
+    // batch scratch: [off | len | prefix] of seg_cap (+1) entries
+    uint64_t* d_seg = nullptr;
+    size_t seg_cap = 0;
+    uint64_t* h_seg = nullptr;  // pinned staging of the same layout
+    cudaEvent_t seg_ev = nullptr;
+    unsigned long long* d_cursor = nullptr;
+    // error-report scratch
+    bsg::ErrAcc* d_acc = nullptr;
+    double* d_edges = nullptr;
+
+    bsg::SoA resident(size_t n) const {
+        (void)n;
+        float* f = reinterpret_cast<float*>(dev_buf);
+        bsg::SoA a;
+        a.s = f;
+        a.k = f + cap_al;
+        a.r = f + 2 * cap_al;
+        a.v = f + 3 * cap_al;
+        a.t = f + 4 * cap_al;
+        a.ot = reinterpret_cast<const int32_t*>(f + 5 * cap_al);
+        a.out = f + 6 * cap_al;
+        return a;
+    }
+};
+
+namespace {
+
+int fail(bsg_ctx* c, int st, const std::string& msg) {
+    if (c) c->err = msg;
+    return st;
+}
+
+int cuda_fail(bsg_ctx* c, cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    if (e == cudaErrorMemoryAllocation) return fail(c, BSG_ERR_OUT_OF_MEMORY, m);
+    return fail(c, BSG_ERR_CUDA, m);
+}
+
+#define BSG_CK(c, call)                                  \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(c, e_, #call); \
+    } while (0)
+
+// cuMemGetAddressRange, resolved through the runtime so that the library has
+// no link-time dependency on libcuda (it loads on machines without a driver).
+typedef CUresult (*MemGetAddressRangeFn)(CUdeviceptr*, size_t*, CUdeviceptr);
+
+MemGetAddressRangeFn mem_get_address_range() {
+    static MemGetAddressRangeFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuMemGetAddressRange", &f, 12000,
+                                             cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            f = nullptr;
+        }
+        return reinterpret_cast<MemGetAddressRangeFn>(f);
+    }();
+    return fn;
+}
+
+// Checks that [p, p + bytes) lies inside one device allocation of the
+// context's device.
+int check_dev_range(bsg_ctx* c, const void* p, size_t bytes, const char* name) {
+    if (!p) return fail(c, BSG_ERR_INVALID_ARG, std::string(name) + " is NULL");
+    if ((reinterpret_cast<uintptr_t>(p) & 3) != 0)
+        return fail(c, BSG_ERR_MISALIGNED, std::string(name) + " is not 4-byte aligned");
+    cudaPointerAttributes attr;
+    cudaError_t e = cudaPointerGetAttributes(&attr, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, BSG_ERR_INVALID_ARG, std::string(name) + " is not a CUDA pointer");
+    }
+    if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
+        return fail(c, BSG_ERR_INVALID_ARG, std::string(name) + " is not device memory");
+    if (attr.type == cudaMemoryTypeDevice && attr.device != c->device)
+        return fail(c, BSG_ERR_INVALID_ARG, std::string(name) + " lives on another device");
+    CUdeviceptr base = 0;
+    size_t size = 0;
+    MemGetAddressRangeFn range = mem_get_address_range();
+    if (!range || range(&base, &size, (CUdeviceptr)p) != CUDA_SUCCESS)
+        return fail(c, BSG_ERR_INVALID_ARG, std::string(name) + ": allocation range unknown");
+    const uintptr_t end = (uintptr_t)base + size;
+    if ((uintptr_t)p + bytes > end || (uintptr_t)p + bytes < (uintptr_t)p)
+        return fail(c, BSG_ERR_INVALID_ARG,
+                    std::string(name) + ": " + std::to_string(bytes) +
+                        " bytes run past the end of its allocation");
+    return BSG_OK;
+}
+
+int check_soa_dev(bsg_ctx* c, const bsg::SoA& a, size_t n, size_t out_elem) {
+    const size_t b = n * 4;
+    int st;
+    if ((st = check_dev_range(c, a.s, b, "sptprice"))) return st;
+    if ((st = check_dev_range(c, a.k, b, "strike"))) return st;
+    if ((st = check_dev_range(c, a.r, b, "rate"))) return st;
+    if ((st = check_dev_range(c, a.v, b, "volatility"))) return st;
+    if ((st = check_dev_range(c, a.t, b, "otime"))) return st;
+    if ((st = check_dev_range(c, a.ot, b, "otype"))) return st;
+    if (out_elem && (st = check_dev_range(c, a.out, n * out_elem, "prices"))) return st;
+    return BSG_OK;
+}
+
+int check_soa_host(bsg_ctx* c, const bsg::SoA& a) {
+    if (!a.s || !a.k || !a.r || !a.v || !a.t || !a.ot || !a.out)
+        return fail(c, BSG_ERR_INVALID_ARG, "a host array is NULL");
+    return BSG_OK;
+}
+
+void graph_drop_all(bsg_ctx* c) {
+    for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+    c->graphs.clear();
+}
+
+cudaGraphExec_t graph_find(bsg_ctx* c, const GraphKey& k) {
+    for (size_t i = 0; i < c->graphs.size(); ++i) {
+        if (c->graphs[i].key == k) {
+            GraphEntry e = c->graphs[i];  // move to front (LRU)
+            c->graphs.erase(c->graphs.begin() + i);
+            c->graphs.insert(c->graphs.begin(), e);
+            return e.exec;
+        }
+    }
+    return nullptr;
+}
+
+void graph_put(bsg_ctx* c, const GraphKey& k, cudaGraphExec_t exec) {
+    if (c->graphs.size() >= kGraphCacheSize) {
+        cudaGraphExecDestroy(c->graphs.back().exec);
+        c->graphs.pop_back();
+    }
+    c->graphs.insert(c->graphs.begin(), GraphEntry{k, exec});
+}
+
+GraphKey make_key(const bsg::SoA& a, int64_t n, int runs, int mode,
+                  const bsg::MapCfg& cfg, int kind, uint64_t ntiles, int nseg) {
+    GraphKey k;
+    std::memset(&k, 0, sizeof(k));  // padding must compare equal
+    k.soa = a;
+    k.n = n;
+    k.runs = runs;
+    k.mode = mode;
+    k.cfg = cfg;
+    k.kind = kind;
+    k.ntiles = ntiles;
+    k.nseg = nseg;
+    return k;
+}
+
+// Enqueues `runs` passes of the plain map on the context stream, from a
+// cached graph when runs > 1 and graphs are allowed.
+int enqueue_map_runs(bsg_ctx* c, const bsg::SoA& a, int64_t n, int runs, int mode,
+                     unsigned flags) {
+    if (n <= 0 || runs <= 0) return BSG_OK;
+    const bsg::MapCfg cfg = c->tune;
+    if (runs == 1 || (flags & BSG_NO_GRAPH)) {
+        for (int j = 0; j < runs; ++j) {
+            cudaError_t e = bsg::launch_map(a, n, mode, cfg, c->sm_count, c->stream);
+            if (e != cudaSuccess) return cuda_fail(c, e, "launch_map");
+            c->launches++;
+        }
+        return BSG_OK;
+    }
+    GraphKey key = make_key(a, n, runs, mode, cfg, 0, 0, 0);
+    cudaGraphExec_t exec = graph_find(c, key);
+    if (!exec) {
+        cudaGraph_t g = nullptr;
+        BSG_CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t le = cudaSuccess;
+        for (int j = 0; j < runs && le == cudaSuccess; ++j)
+            le = bsg::launch_map(a, n, mode, cfg, c->sm_count, c->stream);
+        cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+        if (le != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return cuda_fail(c, le, "launch_map (capture)");
+        }
+        if (ce != cudaSuccess) return cuda_fail(c, ce, "cudaStreamEndCapture");
+        cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) return cuda_fail(c, ie, "cudaGraphInstantiate");
+        graph_put(c, key, exec);
+    }
+    BSG_CK(c, cudaGraphLaunch(exec, c->stream));
+    c->launches += (uint64_t)runs;
+    return BSG_OK;
+}
+
+int finish(bsg_ctx* c, unsigned flags) {
+    if (flags & BSG_ASYNC) return BSG_OK;
+    BSG_CK(c, cudaStreamSynchronize(c->stream));
+    return BSG_OK;
+}
+
+int grow_seg_scratch(bsg_ctx* c, size_t nseg) {
+    if (nseg <= c->seg_cap) return BSG_OK;
+    size_t cap = std::max<size_t>(nseg, 1024);
+    cap = round_up(cap, 1024);
+    if (c->seg_ev) BSG_CK(c, cudaEventSynchronize(c->seg_ev));
+    BSG_CK(c, cudaStreamSynchronize(c->stream));
+    graph_drop_all(c);  // graphs hold the old table address
+    if (c->d_seg) cudaFree(c->d_seg);
+    if (c->h_seg) cudaFreeHost(c->h_seg);
+    c->d_seg = nullptr;
+    c->h_seg = nullptr;
+    c->seg_cap = 0;
+    BSG_CK(c, cudaMalloc(&c->d_seg, (3 * cap + 1) * sizeof(uint64_t)));
+    BSG_CK(c, cudaMallocHost(&c->h_seg, (3 * cap + 1) * sizeof(uint64_t)));
+    c->seg_cap = cap;
+    return BSG_OK;
+}
+
+// Validates the segments and writes the compacted (non-empty) table into the
+// pinned staging buffer.  Returns the count of non-empty segments.
+int build_segments(bsg_ctx* c, const bsg_segment* segs, size_t nseg, size_t pool_len,
+                   uint64_t tile, int* nseg_out, uint64_t* ntiles_out) {
+    std::vector<std::pair<uint64_t, uint64_t>> v;
+    v.reserve(nseg);
+    for (size_t i = 0; i < nseg; ++i) {
+        const uint64_t o = segs[i].offset, l = segs[i].len;
+        if (o > pool_len || l > pool_len - o)
+            return fail(c, BSG_ERR_INVALID_ARG, "segment " + std::to_string(i) + " lies outside the pool");
+        if (l) v.emplace_back(o, l);
+    }
+    std::vector<std::pair<uint64_t, uint64_t>> sorted(v);
+    std::sort(sorted.begin(), sorted.end());
+    for (size_t i = 1; i < sorted.size(); ++i)
+        if (sorted[i - 1].first + sorted[i - 1].second > sorted[i].first)
+            return fail(c, BSG_ERR_INVALID_ARG, "segments overlap");
+    if (v.size() > 0x7fffffff) return fail(c, BSG_ERR_INVALID_ARG, "too many segments");
+    int st = grow_seg_scratch(c, v.size());
+    if (st) return st;
+    if (c->seg_ev) BSG_CK(c, cudaEventSynchronize(c->seg_ev));  // staging reuse
+    const size_t m = v.size();
+    uint64_t* off = c->h_seg;
+    uint64_t* len = c->h_seg + c->seg_cap;
+    uint64_t* pre = c->h_seg + 2 * c->seg_cap;
+    uint64_t acc = 0;
+    for (size_t i = 0; i < m; ++i) {
+        off[i] = v[i].first;
+        len[i] = v[i].second;
+        pre[i] = acc;
+        acc += (v[i].second + tile - 1) / tile;
+    }
+    pre[m] = acc;
+    *nseg_out = (int)m;
+    *ntiles_out = acc;
+    return BSG_OK;
+}
+
+std::mutex g_default_mu;
+bsg_ctx* g_default = nullptr;
+
+}  // namespace
+
+// =================================================================== C ABI
+extern "C" {
+
+const char* bsg_strerror(int status) {
+    switch (status) {
+        case BSG_OK: return "ok";
+        case BSG_ERR_INVALID_ARG: return "invalid argument";
+        case BSG_ERR_NO_DEVICE: return "no usable sm_103 CUDA device";
+        case BSG_ERR_CUDA: return "CUDA runtime error";
+        case BSG_ERR_OUT_OF_MEMORY: return "out of memory";
+        case BSG_ERR_CAPACITY: return "more options than the context capacity";
+        case BSG_ERR_MISALIGNED: return "misaligned pointer";
+        case BSG_ERR_TIMEOUT: return "timed out";
+        case BSG_ERR_BUDGET: return "request exceeds the admission budget";
+        case BSG_ERR_CANCELLED: return "cancelled";
+        case BSG_ERR_NOT_SUPPORTED: return "not supported";
+        case BSG_ERR_STATE: return "invalid state";
+        default: return "unknown status";
+    }
+}
+
+const char* bsg_last_error(const bsg_ctx* ctx) {
+    return ctx ? ctx->err.c_str() : "";
+}
+
+int bsg_create(bsg_ctx** out, int device, size_t max_options) {
+    if (!out) return BSG_ERR_INVALID_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+        cudaGetLastError();
+        return BSG_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= ndev) return BSG_ERR_NO_DEVICE;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return BSG_ERR_NO_DEVICE;
+    if (!(prop.major == 10 && prop.minor == 3)) return BSG_ERR_NO_DEVICE;  // sm_103a cubin only
+    if (max_options > ((size_t)1 << 36)) return BSG_ERR_INVALID_ARG;
+
+    bsg_ctx* c = new (std::nothrow) bsg_ctx();
+    if (!c) return BSG_ERR_OUT_OF_MEMORY;
+    c->device = device;
+    c->sm_count = prop.multiProcessorCount;
+    int rc = BSG_OK;
+    do {
+        if (cudaSetDevice(device) != cudaSuccess) { rc = BSG_ERR_NO_DEVICE; break; }
+        if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { rc = BSG_ERR_CUDA; break; }
+        if (cudaEventCreateWithFlags(&c->seg_ev, cudaEventDisableTiming) != cudaSuccess) { rc = BSG_ERR_CUDA; break; }
+        c->cap = max_options;
+        c->cap_al = round_up(std::max<size_t>(max_options, 1), 64);  // 256-byte aligned arrays
+        if (cudaMalloc(&c->dev_buf, 7 * c->cap_al * sizeof(float)) != cudaSuccess) { rc = BSG_ERR_OUT_OF_MEMORY; break; }
+        if (cudaMalloc(&c->d_cursor, 256) != cudaSuccess) { rc = BSG_ERR_OUT_OF_MEMORY; break; }
+        if (cudaMalloc(&c->d_acc, sizeof(bsg::ErrAcc) * bsg::kMaxErrBuckets) != cudaSuccess) { rc = BSG_ERR_OUT_OF_MEMORY; break; }
+        if (cudaMalloc(&c->d_edges, sizeof(double) * (bsg::kMaxErrBuckets + 1)) != cudaSuccess) { rc = BSG_ERR_OUT_OF_MEMORY; break; }
+        const int bps = bsg::batch_blocks_per_sm();
+        if (bps > 0) c->batch_blocks_per_sm = bps;
+    } while (0);
+    if (rc != BSG_OK) {
+        cudaGetLastError();
+        bsg_destroy(c);
+        return rc;
+    }
+    *out = c;
+    return BSG_OK;
+}
+
+void bsg_destroy(bsg_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    graph_drop_all(c);
+    if (c->dev_buf) cudaFree(c->dev_buf);
+    if (c->d_seg) cudaFree(c->d_seg);
+    if (c->h_seg) cudaFreeHost(c->h_seg);
+    if (c->d_cursor) cudaFree(c->d_cursor);
+    if (c->d_acc) cudaFree(c->d_acc);
+    if (c->d_edges) cudaFree(c->d_edges);
+    if (c->seg_ev) cudaEventDestroy(c->seg_ev);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+void* bsg_stream(bsg_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+uint64_t bsg_kernel_launches(const bsg_ctx* c) { return c ? c->launches : 0; }
+
+void* bsg_host_alloc(size_t bytes) {
+    void* p = nullptr;
+    if (cudaMallocHost(&p, bytes ? bytes : 1) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+void bsg_host_free(void* p) {
+    if (p) cudaFreeHost(p);
+}
+
+int bsg_price_soa(bsg_ctx* c, const float* s, const float* k, const float* r,
+                  const float* v, const float* t, const int32_t* otype,
+                  float* prices, size_t n, int num_runs, unsigned flags) {
+    if (!c) return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mu);
+    try {
+        const int mode = mode_of(flags);
+        if (mode < 0 || num_runs < 0) return fail(c, BSG_ERR_INVALID_ARG, "bad mode flag or num_runs");
+        if (n > ((size_t)1 << 36)) return fail(c, BSG_ERR_INVALID_ARG, "n too large");
+        if (n == 0 || num_runs == 0) return BSG_OK;
+        BSG_CK(c, cudaSetDevice(c->device));
+        bsg::SoA a{s, k, r, v, t, otype, prices};
+        int st;
+        if (flags & BSG_DEVICE_PTRS) {
+            if ((st = check_soa_dev(c, a, n, 4))) return st;
+            if ((st = enqueue_map_runs(c, a, (int64_t)n, num_runs, mode, flags))) return st;
+            return finish(c, flags);
+        }
+        if (flags & BSG_ASYNC) return fail(c, BSG_ERR_INVALID_ARG, "BSG_ASYNC needs device pointers");
+        if ((st = check_soa_host(c, a))) return st;
+        if (n > c->cap) return fail(c, BSG_ERR_CAPACITY, "n exceeds the context's max_options");
+        const bsg::SoA d = c->resident(n);
+        const size_t b = n * 4;
+        BSG_CK(c, cudaMemcpyAsync((void*)d.s, s, b, cudaMemcpyHostToDevice, c->stream));
+        BSG_CK(c, cudaMemcpyAsync((void*)d.k, k, b, cudaMemcpyHostToDevice, c->stream));
+        BSG_CK(c, cudaMemcpyAsync((void*)d.r, r, b, cudaMemcpyHostToDevice, c->stream));
+        BSG_CK(c, cudaMemcpyAsync((void*)d.v, v, b, cudaMemcpyHostToDevice, c->stream));
+        BSG_CK(c, cudaMemcpyAsync((void*)d.t, t, b, cudaMemcpyHostToDevice, c->stream));
+        BSG_CK(c, cudaMemcpyAsync((void*)d.ot, otype, b, cudaMemcpyHostToDevice, c->stream));
+        if ((st = enqueue_map_runs(c, d, (int64_t)n, num_runs, mode, flags))) return st;
+        BSG_CK(c, cudaMemcpyAsync(prices, d.out, b, cudaMemcpyDeviceToHost, c->stream));
+        BSG_CK(c, cudaStreamSynchronize(c->stream));
+        return BSG_OK;
+    } catch (const std::bad_alloc&) {
+        return fail(c, BSG_ERR_OUT_OF_MEMORY, "host allocation failed");
+    }
+}
+
+int bsg_BlkSchlsEqEuroNoDiv(float* OptionPrice, int numOptions, float* sptprice,
+                            float* strike, float* rate, float* volatility,
+                            float* time, int* otype, float timet) {
+    (void)timet;  // unused by the reference too
+    if (numOptions < 0) return BSG_ERR_INVALID_ARG;
+    if (numOptions == 0) return BSG_OK;
+    std::lock_guard<std::mutex> lk(g_default_mu);
+    if (!g_default || g_default->cap < (size_t)numOptions) {
+        if (g_default) bsg_destroy(g_default);
+        g_default = nullptr;
+        size_t cap = std::max<size_t>((size_t)numOptions, (size_t)1 << 16);
+        int st = bsg_create(&g_default, 0, cap);
+        if (st) return st;
+    }
+    return bsg_price_soa(g_default, sptprice, strike, rate, volatility, time,
+                         (const int32_t*)otype, OptionPrice, (size_t)numOptions, 1,
+                         BSG_HOST_PTRS);
+}
+
+int bsg_price_fp64(bsg_ctx* c, const float* s, const float* k, const float* r,
+                   const float* v, const float* t, const int32_t* otype,
+                   double* out, size_t n, unsigned flags) {
+    if (!c) return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (n == 0) return BSG_OK;
+    if (n > ((size_t)1 << 36)) return fail(c, BSG_ERR_INVALID_ARG, "n too large");
+    BSG_CK(c, cudaSetDevice(c->device));
+    bsg::SoA a{s, k, r, v, t, otype, nullptr};
+    int st;
+    if (flags & BSG_DEVICE_PTRS) {
+        if ((st = check_soa_dev(c, a, n, 0))) return st;
+        if ((st = check_dev_range(c, out, n * 8, "out"))) return st;
+        cudaError_t e = bsg::launch_fp64(a, out, (int64_t)n, c->sm_count, c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "launch_fp64");
+        c->launches++;
+        return finish(c, flags);
+    }
+    if (!s || !k || !r || !v || !t || !otype || !out)
+        return fail(c, BSG_ERR_INVALID_ARG, "a host array is NULL");
+    if (n > c->cap) return fail(c, BSG_ERR_CAPACITY, "n exceeds the context's max_options");
+    const bsg::SoA d = c->resident(n);
+    const size_t b = n * 4;
+    double* dout = nullptr;
+    BSG_CK(c, cudaMalloc(&dout, n * 8));
+    std::unique_ptr<double, decltype(&cudaFree)> guard(dout, &cudaFree);
+    BSG_CK(c, cudaMemcpyAsync((void*)d.s, s, b, cudaMemcpyHostToDevice, c->stream));
+    BSG_CK(c, cudaMemcpyAsync((void*)d.k, k, b, cudaMemcpyHostToDevice, c->stream));
+    BSG_CK(c, cudaMemcpyAsync((void*)d.r, r, b, cudaMemcpyHostToDevice, c->stream));
+    BSG_CK(c, cudaMemcpyAsync((void*)d.v, v, b, cudaMemcpyHostToDevice, c->stream));
+    BSG_CK(c, cudaMemcpyAsync((void*)d.t, t, b, cudaMemcpyHostToDevice, c->stream));
+    BSG_CK(c, cudaMemcpyAsync((void*)d.ot, otype, b, cudaMemcpyHostToDevice, c->stream));
+    cudaError_t e = bsg::launch_fp64(d, dout, (int64_t)n, c->sm_count, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "launch_fp64");
+    c->launches++;
+    BSG_CK(c, cudaMemcpyAsync(out, dout, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    BSG_CK(c, cudaStreamSynchronize(c->stream));
+    return BSG_OK;
+}
+
+int bsg_price_batch(bsg_ctx* c, const float* s, const float* k, const float* r,
+                    const float* v, const float* t, const int32_t* otype,
+                    float* prices, size_t pool_len, const bsg_segment* segs,
+                    size_t nseg, int num_runs, unsigned flags) {
+    if (!c) return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mu);
+    try {
+        const int mode = mode_of(flags);
+        if (mode < 0 || num_runs < 0) return fail(c, BSG_ERR_INVALID_ARG, "bad mode flag or num_runs");
+        if (!(flags & BSG_DEVICE_PTRS)) return fail(c, BSG_ERR_NOT_SUPPORTED, "batch pools must be device memory");
+        if (nseg && !segs) return fail(c, BSG_ERR_INVALID_ARG, "segs is NULL");
+        if (pool_len == 0 || nseg == 0 || num_runs == 0) return BSG_OK;
+        BSG_CK(c, cudaSetDevice(c->device));
+        bsg::SoA a{s, k, r, v, t, otype, prices};
+        int st;
+        if ((st = check_soa_dev(c, a, pool_len, 4))) return st;
+        if ((reinterpret_cast<uintptr_t>(s) | reinterpret_cast<uintptr_t>(k) |
+             reinterpret_cast<uintptr_t>(r) | reinterpret_cast<uintptr_t>(v) |
+             reinterpret_cast<uintptr_t>(t) | reinterpret_cast<uintptr_t>(otype) |
+             reinterpret_cast<uintptr_t>(prices)) & 15)
+            return fail(c, BSG_ERR_MISALIGNED, "batch pool arrays must be 16-byte aligned");
+        int m = 0;
+        uint64_t ntiles = 0;
+        if ((st = build_segments(c, segs, nseg, pool_len, bsg::batch_tile_options(), &m, &ntiles))) return st;
+        if (m == 0) return finish(c, flags);
+        const uint64_t* d_off = c->d_seg;
+        const uint64_t* d_len = c->d_seg + c->seg_cap;
+        const uint64_t* d_pre = c->d_seg + 2 * c->seg_cap;
+        // table upload (3 copies of the used prefix of each array)
+        BSG_CK(c, cudaMemcpyAsync((void*)d_off, c->h_seg, m * 8, cudaMemcpyHostToDevice, c->stream));
+        BSG_CK(c, cudaMemcpyAsync((void*)d_len, c->h_seg + c->seg_cap, m * 8, cudaMemcpyHostToDevice, c->stream));
+        BSG_CK(c, cudaMemcpyAsync((void*)d_pre, c->h_seg + 2 * c->seg_cap, (m + 1) * 8, cudaMemcpyHostToDevice, c->stream));
+        BSG_CK(c, cudaEventRecord(c->seg_ev, c->stream));
+        const int grid = c->sm_count * c->batch_blocks_per_sm;
+        auto one_run = [&]() -> cudaError_t {
+            cudaError_t e = cudaMemsetAsync(c->d_cursor, 0, sizeof(unsigned long long), c->stream);
+            if (e != cudaSuccess) return e;
+            return bsg::launch_batch(a, d_off, d_len, d_pre, m, ntiles, c->d_cursor, mode, grid, c->stream);
+        };
+        if (num_runs == 1 || (flags & BSG_NO_GRAPH)) {
+            for (int j = 0; j < num_runs; ++j) {
+                cudaError_t e = one_run();
+                if (e != cudaSuccess) return cuda_fail(c, e, "launch_batch");
+                c->launches++;
+            }
+            return finish(c, flags);
+        }
+        GraphKey key = make_key(a, (int64_t)pool_len, num_runs, mode, c->tune, 1, ntiles, m);
+        cudaGraphExec_t exec = graph_find(c, key);
+        if (!exec) {
+            cudaGraph_t g = nullptr;
+            BSG_CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            cudaError_t le = cudaSuccess;
+            for (int j = 0; j < num_runs && le == cudaSuccess; ++j) le = one_run();
+            cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+            if (le != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                return cuda_fail(c, le, "launch_batch (capture)");
+            }
+            if (ce != cudaSuccess) return cuda_fail(c, ce, "cudaStreamEndCapture");
+            cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
+            cudaGraphDestroy(g);
+            if (ie != cudaSuccess) return cuda_fail(c, ie, "cudaGraphInstantiate");
+            graph_put(c, key, exec);
+        }
+        BSG_CK(c, cudaGraphLaunch(exec, c->stream));
+        c->launches += (uint64_t)num_runs;
+        return finish(c, flags);
+    } catch (const std::bad_alloc&) {
+        return fail(c, BSG_ERR_OUT_OF_MEMORY, "host allocation failed");
+    }
+}
+
+int bsg_price_books_plain(bsg_ctx* c, const float* s, const float* k, const float* r,
+                          const float* v, const float* t, const int32_t* otype,
+                          float* prices, size_t pool_len, const bsg_segment* segs,
+                          size_t nseg, int num_runs, unsigned flags) {
+    if (!c) return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mu);
+    const int mode = mode_of(flags);
+    if (mode < 0 || num_runs < 0) return fail(c, BSG_ERR_INVALID_ARG, "bad mode flag or num_runs");
+    if (!(flags & BSG_DEVICE_PTRS)) return fail(c, BSG_ERR_NOT_SUPPORTED, "batch pools must be device memory");
+    if (nseg && !segs) return fail(c, BSG_ERR_INVALID_ARG, "segs is NULL");
+    if (pool_len == 0 || nseg == 0 || num_runs == 0) return BSG_OK;
+    BSG_CK(c, cudaSetDevice(c->device));
+    bsg::SoA a{s, k, r, v, t, otype, prices};
+    int st;
+    if ((st = check_soa_dev(c, a, pool_len, 4))) return st;
+    for (size_t i = 0; i < nseg; ++i) {
+        const uint64_t o = segs[i].offset, l = segs[i].len;
+        if (o > pool_len || l > pool_len - o)
+            return fail(c, BSG_ERR_INVALID_ARG, "segment " + std::to_string(i) + " lies outside the pool");
+    }
+    for (int j = 0; j < num_runs; ++j) {
+        for (size_t i = 0; i < nseg; ++i) {
+            if (!segs[i].len) continue;
+            const uint64_t o = segs[i].offset;
+            bsg::SoA b{s + o, k + o, r + o, v + o, t + o, otype + o, prices + o};
+            cudaError_t e = bsg::launch_map(b, (int64_t)segs[i].len, mode, c->tune, c->sm_count, c->stream);
+            if (e != cudaSuccess) return cuda_fail(c, e, "launch_map (per book)");
+            c->launches++;
+        }
+    }
+    return finish(c, flags);
+}
+
+int bsg_error_report(bsg_ctx* c, const float* s, const float* k, const float* r,
+                     const float* v, const float* t, const int32_t* otype,
+                     const float* prices, size_t n, const double* edges,
+                     int nbuckets, double rel_floor, bsg_err_bucket* out) {
+    if (!c) return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (!edges || !out || nbuckets < 1 || nbuckets > BSG_MAX_ERR_BUCKETS)
+        return fail(c, BSG_ERR_INVALID_ARG, "bad bucket arguments");
+    for (int i = 0; i < nbuckets; ++i)
+        if (!(edges[i] < edges[i + 1])) return fail(c, BSG_ERR_INVALID_ARG, "bucket edges must ascend");
+    BSG_CK(c, cudaSetDevice(c->device));
+    bsg::SoA a{s, k, r, v, t, otype, nullptr};
+    int st;
+    if (n) {
+        if ((st = check_soa_dev(c, a, n, 0))) return st;
+        if ((st = check_dev_range(c, prices, n * 4, "prices"))) return st;
+    }
+    BSG_CK(c, cudaMemsetAsync(c->d_acc, 0, sizeof(bsg::ErrAcc) * nbuckets, c->stream));
+    BSG_CK(c, cudaMemcpyAsync(c->d_edges, edges, sizeof(double) * (nbuckets + 1), cudaMemcpyHostToDevice, c->stream));
+    if (n) {
+        cudaError_t e = bsg::launch_err_report(a, prices, (int64_t)n, c->d_edges, nbuckets,
+                                               rel_floor, c->d_acc, c->sm_count, c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "launch_err_report");
+        c->launches++;
+    }
+    std::vector<bsg::ErrAcc> h(nbuckets);
+    BSG_CK(c, cudaMemcpyAsync(h.data(), c->d_acc, sizeof(bsg::ErrAcc) * nbuckets, cudaMemcpyDeviceToHost, c->stream));
+    BSG_CK(c, cudaStreamSynchronize(c->stream));
+    for (int i = 0; i < nbuckets; ++i) {
+        out[i].count = h[i].count;
+        long long b;
+        std::memcpy(&b, &h[i].max_abs_bits, 8); std::memcpy(&out[i].max_abs, &b, 8);
+        std::memcpy(&b, &h[i].max_rel_bits, 8); std::memcpy(&out[i].max_rel, &b, 8);
+        std::memcpy(&b, &h[i].max_price_bits, 8); std::memcpy(&out[i].max_price, &b, 8);
+        out[i].sum_sq_abs = h[i].sum_sq;
+    }
+    return BSG_OK;
+}
+
+int bsg_get_tune(const bsg_ctx* c, bsg_tune* out) {
+    if (!c || !out) return BSG_ERR_INVALID_ARG;
+    out->vec_per_thread = c->tune.vpt;
+    out->block = c->tune.block;
+    out->blocks_per_sm = c->tune.blocks_per_sm;
+    out->load_path = c->tune.load_path;
+    return BSG_OK;
+}
+
+static bool tune_valid(const bsg_tune* t) {
+    const bool vpt_ok = t->vec_per_thread == 1 || t->vec_per_thread == 2 ||
+                        (t->vec_per_thread == 4 && t->load_path != 2);
+    const bool blk_ok = t->block == 128 || t->block == 256 || t->block == 512;
+    return vpt_ok && blk_ok && t->blocks_per_sm >= 0 && t->blocks_per_sm <= 64 &&
+           t->load_path >= 0 && t->load_path <= 2;
+}
+
+int bsg_set_tune(bsg_ctx* c, const bsg_tune* t) {
+    if (!c || !t) return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (!tune_valid(t)) return fail(c, BSG_ERR_INVALID_ARG, "unsupported tuning");
+    c->tune = bsg::MapCfg{t->vec_per_thread, t->block, t->blocks_per_sm, t->load_path};
+    return BSG_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------- autotuner
+// Times every plain-map shape on the context's device for n options and
+// keeps the fastest.  The choice is cached per (device name, SM count,
+// floor(log2 n)) in $BSG_TUNE_CACHE when that variable names a file.
+static std::string tune_key(const bsg_ctx* c, size_t n) {
+    cudaDeviceProp p;
+    cudaGetDeviceProperties(&p, c->device);
+    int b = 0;
+    while (((size_t)1 << (b + 1)) <= n) ++b;
+    std::ostringstream os;
+    os << p.name << "|" << p.multiProcessorCount << "|" << b;
+    return os.str();
+}
+
+static bool tune_cache_lookup(const std::string& key, bsg_tune* t) {
+    const char* path = std::getenv("BSG_TUNE_CACHE");
+    if (!path || !*path) return false;
+    std::ifstream f(path);
+    std::string line;
+    bool found = false;
+    while (std::getline(f, line)) {
+        const size_t bar = line.rfind('|');
+        if (bar == std::string::npos || line.compare(0, bar, key) != 0) continue;
+        bsg_tune x;
+        if (std::sscanf(line.c_str() + bar + 1, "%d %d %d %d", &x.vec_per_thread, &x.block,
+                        &x.blocks_per_sm, &x.load_path) == 4 && tune_valid(&x)) {
+            *t = x;
+            found = true;
+        }
+    }
+    return found;
+}
+
+static void tune_cache_store(const std::string& key, const bsg_tune& t) {
+    const char* path = std::getenv("BSG_TUNE_CACHE");
+    if (!path || !*path) return;
+    std::ofstream f(path, std::ios::app);
+    f << key << "|" << t.vec_per_thread << " " << t.block << " " << t.blocks_per_sm << " "
+      << t.load_path << "\n";
+}
+
+extern "C" int bsg_autotune(bsg_ctx* c, size_t n, bsg_tune* out) {
+    if (!c || n == 0) return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mu);
+    BSG_CK(c, cudaSetDevice(c->device));
+    const std::string key = tune_key(c, n);
+    bsg_tune best{};
+    if (tune_cache_lookup(key, &best)) {
+        c->tune = bsg::MapCfg{best.vec_per_thread, best.block, best.blocks_per_sm, best.load_path};
+        if (out) *out = best;
+        return BSG_OK;
+    }
+    // inputs: the resident buffers when they fit, else a temporary pool
+    bsg::SoA a;
+    char* tmp = nullptr;
+    if (n <= c->cap) {
+        a = c->resident(n);
+    } else {
+        const size_t al = round_up(n, 64);
+        BSG_CK(c, cudaMalloc(&tmp, 7 * al * sizeof(float)));
+        float* f = reinterpret_cast<float*>(tmp);
+        a = bsg::SoA{f, f + al, f + 2 * al, f + 3 * al, f + 4 * al,
+                     reinterpret_cast<const int32_t*>(f + 5 * al), f + 6 * al};
+    }
+    std::unique_ptr<char, decltype(&cudaFree)> guard(tmp, &cudaFree);
+    cudaError_t e = bsg::launch_fill(a, (int64_t)n, 12345u, c->sm_count, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "launch_fill");
+    c->launches++;
+    cudaEvent_t e0, e1;
+    BSG_CK(c, cudaEventCreate(&e0));
+    BSG_CK(c, cudaEventCreate(&e1));
+    float best_ms = 1e30f;
+    const int reps = 3;
+    for (int lp = 0; lp <= 2; ++lp)
+        for (int vpt : {1, 2, 4})
+            for (int block : {128, 256, 512})
+                for (int bps : {0, 2, 4, 8}) {
+                    bsg_tune t{vpt, block, bps, lp};
+                    if (!tune_valid(&t)) continue;
+                    const bsg::MapCfg cfg{vpt, block, bps, lp};
+                    e = bsg::launch_map(a, (int64_t)n, bsg::MODE_FAST, cfg, c->sm_count, c->stream);
+                    if (e != cudaSuccess) break;
+                    cudaEventRecord(e0, c->stream);
+                    for (int i = 0; i < reps && e == cudaSuccess; ++i)
+                        e = bsg::launch_map(a, (int64_t)n, bsg::MODE_FAST, cfg, c->sm_count, c->stream);
+                    cudaEventRecord(e1, c->stream);
+                    c->launches += reps + 1;
+                    if (e != cudaSuccess) break;
+                    cudaEventSynchronize(e1);
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (ms < best_ms) {
+                        best_ms = ms;
+                        best = t;
+                    }
+                }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return cuda_fail(c, e, "autotune launch");
+    BSG_CK(c, cudaStreamSynchronize(c->stream));
+    c->tune = bsg::MapCfg{best.vec_per_thread, best.block, best.blocks_per_sm, best.load_path};
+    tune_cache_store(key, best);
+    if (out) *out = best;
+    return BSG_OK;
+}

@@ -1,0 +1,75 @@
+// bsg_internal.h -- launch interface between the C ABI (bsg_api.cu) and the
+// kernels (bsg_kernels.cu).  Not installed; no torch types anywhere.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace bsg {
+
+// Arithmetic of the map (see bsg_math.cuh).
+enum Mode : int { MODE_FAST = 0, MODE_SFU_REF = 1, MODE_LIBM_REF = 2 };
+
+// One SoA view: the reference's five float arrays, int32 otype, float out.
+struct SoA {
+    const float* s;
+    const float* k;
+    const float* r;
+    const float* v;
+    const float* t;
+    const int32_t* ot;
+    float* out;
+};
+
+// Plain-map launch shape (see bsg_tune in bsg.h).
+struct MapCfg {
+    int vpt;           // vector groups per thread per tile: 1, 2, 4
+    int block;         // threads per block
+    int blocks_per_sm; // 0: one block per tile; else grid = blocks_per_sm * SMs
+    int load_path;     // 0: v4 nc; 1: v4 + L2 evict_first; 2: v8 (256-bit) nc
+};
+
+// Accumulators of one error bucket (device scratch, zeroed per report).
+struct ErrAcc {
+    unsigned long long count;
+    unsigned long long max_abs_bits;   // non-negative doubles order as u64
+    unsigned long long max_rel_bits;
+    unsigned long long max_price_bits;
+    double sum_sq;
+};
+
+constexpr int kMaxErrBuckets = 32;
+constexpr int kBatchBlock = 256;
+
+// Launches one pass of the plain map over n options.  Picks the vector
+// kernel when every pointer is aligned for the configured width, else the
+// scalar kernel.  Returns the launch error.
+cudaError_t launch_map(const SoA& a, int64_t n, int mode, const MapCfg& cfg,
+                       int sm_count, cudaStream_t st);
+// True when launch_map would take the vector path for these pointers.
+bool map_vectorizable(const SoA& a, const MapCfg& cfg);
+
+cudaError_t launch_fp64(const SoA& a, double* out, int64_t n, int sm_count,
+                        cudaStream_t st);
+
+// Persistent batched pricing.  seg_off/seg_len/tile_prefix are device arrays
+// of nseg (tile_prefix: nseg + 1 entries, exclusive prefix of tiles per
+// segment); cursor is a device counter that must be 0 at launch.
+cudaError_t launch_batch(const SoA& pool, const uint64_t* seg_off,
+                         const uint64_t* seg_len, const uint64_t* tile_prefix,
+                         int nseg, uint64_t ntiles, unsigned long long* cursor,
+                         int mode, int grid, cudaStream_t st);
+// Options per batch tile (fixed by the batch kernel's shape).
+uint64_t batch_tile_options();
+// Resident blocks per SM of the batch kernel (its persistent grid = this x SMs).
+int batch_blocks_per_sm();
+
+cudaError_t launch_err_report(const SoA& a, const float* prices, int64_t n,
+                              const double* edges, int nbuckets,
+                              double rel_floor, ErrAcc* acc, int sm_count,
+                              cudaStream_t st);
+
+// Fills n options with a deterministic plausible book (autotuning input).
+cudaError_t launch_fill(const SoA& a, int64_t n, uint32_t seed, int sm_count,
+                        cudaStream_t st);
+
+}  // namespace bsg

@@ -1,0 +1,411 @@
+// bsg_kernels.cu -- sm_103a kernels of the Black-Scholes map.
+//
+// The hot path is an HBM-bound elementwise map: 28 bytes per option per run
+// (five float inputs, one int32 otype, one float price) against ~100 FP32/SFU
+// instructions.  Design:
+//  * SoA streams read with 128-bit (v4) or 256-bit (v8) non-coherent loads
+//    that do not allocate in L1; prices stored with streaming stores.
+//  * Each thread loads VPT vector groups of all six arrays before computing,
+//    so a warp keeps 6 * VPT independent 512/1024-byte requests in flight.
+//  * Grid: one block per tile, or a persistent grid-stride loop sized in
+//    multiples of the SM count (chosen by the autotuner).
+//  * No shared memory, no tensor cores: there is no reuse to stage and no
+//    contraction to run.
+#include "bsg_internal.h"
+#include "bsg_math.cuh"
+
+namespace bsg {
+
+// ------------------------------------------------------------ memory access
+__device__ __forceinline__ unsigned long long evict_first_policy() {
+    unsigned long long pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+template <int W>
+struct Raw {
+    uint32_t v[W];
+};
+
+// LP 0/2: ld.global.nc.L1::no_allocate (v4 / v8); LP 1: v4 plus an L2
+// evict_first cache policy.
+template <int W, int LP>
+__device__ __forceinline__ Raw<W> ld_group(const void* p, unsigned long long pol) {
+    Raw<W> r;
+    if constexpr (W == 4) {
+        if constexpr (LP == 1) {
+            asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
+                : "=r"(r.v[0]), "=r"(r.v[1]), "=r"(r.v[2]), "=r"(r.v[3])
+                : "l"(p), "l"(pol));
+        } else {
+            (void)pol;
+            asm("ld.global.nc.L1::no_allocate.v4.u32 {%0,%1,%2,%3}, [%4];"
+                : "=r"(r.v[0]), "=r"(r.v[1]), "=r"(r.v[2]), "=r"(r.v[3])
+                : "l"(p));
+        }
+    } else {
+        (void)pol;
+        asm("ld.global.nc.L1::no_allocate.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+            : "=r"(r.v[0]), "=r"(r.v[1]), "=r"(r.v[2]), "=r"(r.v[3]),
+              "=r"(r.v[4]), "=r"(r.v[5]), "=r"(r.v[6]), "=r"(r.v[7])
+            : "l"(p));
+    }
+    return r;
+}
+
+template <int W>
+__device__ __forceinline__ void st_group(float* p, const float (&x)[W]) {
+    if constexpr (W == 4) {
+        asm volatile("st.global.cs.v4.f32 [%0], {%1,%2,%3,%4};"
+                     :: "l"(p), "f"(x[0]), "f"(x[1]), "f"(x[2]), "f"(x[3])
+                     : "memory");
+    } else {
+        asm volatile("st.global.cs.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};"
+                     :: "l"(p), "f"(x[0]), "f"(x[1]), "f"(x[2]), "f"(x[3]),
+                        "f"(x[4]), "f"(x[5]), "f"(x[6]), "f"(x[7])
+                     : "memory");
+    }
+}
+
+
+template <int M>
+__device__ __forceinline__ void price_scalar(const SoA& a, int64_t i) {
+    a.out[i] = price<M>(__ldg(a.s + i), __ldg(a.k + i), __ldg(a.r + i),
+                        __ldg(a.v + i), __ldg(a.t + i), __ldg(a.ot + i));
+}
+
+// Prices vector groups [g0, g1) (group = W options) of one block's range:
+// each thread loads VPT groups (stride blockDim.x) of all six arrays, then
+// computes and stores them.
+template <int M, int W, int VPT, int LP>
+__device__ __forceinline__ void price_groups(const SoA& a, int64_t g0, int64_t g1,
+                                             unsigned long long pol) {
+    const int64_t bd = blockDim.x;
+    for (int64_t base = g0; base < g1; base += bd * VPT) {
+        Raw<W> S[VPT], K[VPT], R[VPT], V[VPT], T[VPT], O[VPT];
+#pragma unroll
+        for (int j = 0; j < VPT; ++j) {
+            const int64_t g = base + threadIdx.x + j * bd;
+            if (g < g1) {
+                const int64_t o = g * W;
+                S[j] = ld_group<W, LP>(a.s + o, pol);
+                K[j] = ld_group<W, LP>(a.k + o, pol);
+                R[j] = ld_group<W, LP>(a.r + o, pol);
+                V[j] = ld_group<W, LP>(a.v + o, pol);
+                T[j] = ld_group<W, LP>(a.t + o, pol);
+                O[j] = ld_group<W, LP>(a.ot + o, pol);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < VPT; ++j) {
+            const int64_t g = base + threadIdx.x + j * bd;
+            if (g < g1) {
+                float p[W];
+#pragma unroll
+                for (int e = 0; e < W; ++e)
+                    p[e] = price<M>(__uint_as_float(S[j].v[e]), __uint_as_float(K[j].v[e]),
+                                    __uint_as_float(R[j].v[e]), __uint_as_float(V[j].v[e]),
+                                    __uint_as_float(T[j].v[e]), (int)O[j].v[e]);
+                st_group<W>(a.out + g * W, p);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------- plain map
+// Vector kernel: options [0, n - n % W) in groups of W; the last n % W
+// options by block 0.  blocks_per_sm == 0: each block prices one tile of
+// blockDim.x * VPT groups; otherwise blocks stride over tiles.
+template <int M, int W, int VPT, int LP>
+__global__ void __launch_bounds__(512) map_vec_kernel(SoA a, int64_t n) {
+    const unsigned long long pol = (LP == 1) ? evict_first_policy() : 0ull;
+    const int64_t ngroups = n / W;
+    const int64_t tile = (int64_t)blockDim.x * VPT;
+    for (int64_t t0 = (int64_t)blockIdx.x * tile; t0 < ngroups; t0 += (int64_t)gridDim.x * tile) {
+        const int64_t t1 = (t0 + tile < ngroups) ? t0 + tile : ngroups;
+        price_groups<M, W, VPT, LP>(a, t0, t1, pol);
+    }
+    if (blockIdx.x == 0) {
+        const int64_t i = ngroups * W + threadIdx.x;
+        if (i < n) price_scalar<M>(a, i);
+    }
+}
+
+// Scalar kernel: any 4-byte aligned pointers.
+template <int M>
+__global__ void __launch_bounds__(256) map_scalar_kernel(SoA a, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        price_scalar<M>(a, i);
+}
+
+static bool aligned(const void* p, uintptr_t al) {
+    return (reinterpret_cast<uintptr_t>(p) & (al - 1)) == 0;
+}
+
+bool map_vectorizable(const SoA& a, const MapCfg& cfg) {
+    const uintptr_t al = (cfg.load_path == 2) ? 32 : 16;
+    return aligned(a.s, al) && aligned(a.k, al) && aligned(a.r, al) &&
+           aligned(a.v, al) && aligned(a.t, al) && aligned(a.ot, al) &&
+           aligned(a.out, al);
+}
+
+template <int M>
+static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg,
+                                   int sm_count, cudaStream_t st) {
+    const int block = cfg.block;
+    if (!map_vectorizable(a, cfg)) {
+        int64_t grid = (n + 255) / 256;
+        const int64_t cap = (int64_t)sm_count * 8;
+        if (grid > cap) grid = cap;
+        if (grid < 1) grid = 1;
+        map_scalar_kernel<M><<<(unsigned)grid, 256, 0, st>>>(a, n);
+        return cudaGetLastError();
+    }
+    const int W = (cfg.load_path == 2) ? 8 : 4;
+    const int64_t ngroups = n / W;
+    const int64_t tile = (int64_t)block * cfg.vpt;
+    int64_t ntiles = (ngroups + tile - 1) / tile;
+    int64_t grid = ntiles;
+    if (cfg.blocks_per_sm > 0) {
+        const int64_t cap = (int64_t)cfg.blocks_per_sm * sm_count;
+        if (grid > cap) grid = cap;
+    }
+    if (grid > 0x7fffffff) grid = 0x7fffffff;
+    if (grid < 1) grid = 1;
+    const dim3 g((unsigned)grid), b((unsigned)block);
+
+#define BSG_LAUNCH(W_, V_, L_) map_vec_kernel<M, W_, V_, L_><<<g, b, 0, st>>>(a, n)
+    if constexpr (M == MODE_FAST) {
+        switch (cfg.load_path * 10 + cfg.vpt) {
+            case 1: BSG_LAUNCH(4, 1, 0); break;
+            case 2: BSG_LAUNCH(4, 2, 0); break;
+            case 4: BSG_LAUNCH(4, 4, 0); break;
+            case 11: BSG_LAUNCH(4, 1, 1); break;
+            case 12: BSG_LAUNCH(4, 2, 1); break;
+            case 14: BSG_LAUNCH(4, 4, 1); break;
+            case 21: BSG_LAUNCH(8, 1, 2); break;
+            case 22: BSG_LAUNCH(8, 2, 2); break;
+            default: return cudaErrorInvalidValue;
+        }
+    } else {
+        // reference-order paths are validation variants: one shape.
+        if (cfg.load_path == 2) BSG_LAUNCH(8, 1, 2);
+        else BSG_LAUNCH(4, 1, 0);
+    }
+#undef BSG_LAUNCH
+    return cudaGetLastError();
+}
+
+cudaError_t launch_map(const SoA& a, int64_t n, int mode, const MapCfg& cfg,
+                       int sm_count, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (cfg.block < 32 || cfg.block > 512 || (cfg.block & 31)) return cudaErrorInvalidValue;
+    switch (mode) {
+        case MODE_FAST: return launch_map_mode<MODE_FAST>(a, n, cfg, sm_count, st);
+        case MODE_SFU_REF: return launch_map_mode<MODE_SFU_REF>(a, n, cfg, sm_count, st);
+        case MODE_LIBM_REF: return launch_map_mode<MODE_LIBM_REF>(a, n, cfg, sm_count, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+// ------------------------------------------------------------------ FP64
+__global__ void __launch_bounds__(256) fp64_kernel(SoA a, double* out, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = price_fp64(a.s[i], a.k[i], a.r[i], a.v[i], a.t[i], a.ot[i]);
+}
+
+cudaError_t launch_fp64(const SoA& a, double* out, int64_t n, int sm_count,
+                        cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    int64_t grid = (n + 255) / 256;
+    const int64_t cap = (int64_t)sm_count * 8;
+    if (grid > cap) grid = cap;
+    fp64_kernel<<<(unsigned)grid, 256, 0, st>>>(a, out, n);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ batched books
+// A tile is 8192 options; a block covers it in passes of kBatchBlock
+// threads x kBatchVpt v4 groups.
+constexpr int kBatchVpt = 2;
+constexpr uint64_t kBatchTileOptions = 8192;
+
+uint64_t batch_tile_options() { return kBatchTileOptions; }
+
+// Prices options [b, e) of the pool with the whole block: an unaligned head
+// and tail one option per thread, the 16-byte aligned body in v4 groups.
+template <int M>
+__device__ __forceinline__ void price_range(const SoA& pool, uint64_t b, uint64_t e) {
+    const uint64_t head_end = ((b + 3) & ~3ull) < e ? ((b + 3) & ~3ull) : e;
+    const uint64_t body_end = (e & ~3ull) > head_end ? (e & ~3ull) : head_end;
+    const uint64_t i_head = b + threadIdx.x;
+    if (i_head < head_end) price_scalar<M>(pool, (int64_t)i_head);
+    price_groups<M, 4, kBatchVpt, 0>(pool, (int64_t)(head_end / 4), (int64_t)(body_end / 4), 0ull);
+    const uint64_t i_tail = body_end + threadIdx.x;
+    if (i_tail < e) price_scalar<M>(pool, (int64_t)i_tail);
+}
+
+// Persistent kernel: each block takes the next tile from the device work
+// counter, maps it to its segment by binary search over the tile prefix and
+// prices it.  No block ever waits on another; the loop ends when the counter
+// passes the last tile.
+template <int M>
+__global__ void __launch_bounds__(kBatchBlock) batch_kernel(
+    SoA pool, const uint64_t* __restrict__ seg_off, const uint64_t* __restrict__ seg_len,
+    const uint64_t* __restrict__ tile_prefix, int nseg, uint64_t ntiles,
+    unsigned long long* cursor) {
+    __shared__ uint64_t sh_b, sh_e;
+    __shared__ int sh_done;
+    const uint64_t topt = kBatchTileOptions;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const unsigned long long tile = atomicAdd(cursor, 1ull);
+            if (tile >= ntiles) {
+                sh_done = 1;
+            } else {
+                int lo = 0, hi = nseg - 1;
+                while (lo < hi) {  // largest segment whose first tile <= tile
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (tile_prefix[mid] <= tile) lo = mid; else hi = mid - 1;
+                }
+                const uint64_t b = seg_off[lo] + (tile - tile_prefix[lo]) * topt;
+                const uint64_t send = seg_off[lo] + seg_len[lo];
+                sh_b = b;
+                sh_e = (b + topt < send) ? b + topt : send;
+                sh_done = 0;
+            }
+        }
+        __syncthreads();
+        const int done = sh_done;
+        const uint64_t b = sh_b, e = sh_e;
+        __syncthreads();
+        if (done) break;
+        price_range<M>(pool, b, e);
+    }
+}
+
+int batch_blocks_per_sm() {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<MODE_FAST>, kBatchBlock, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return n > 0 ? n : 1;
+}
+
+cudaError_t launch_batch(const SoA& pool, const uint64_t* seg_off,
+                         const uint64_t* seg_len, const uint64_t* tile_prefix,
+                         int nseg, uint64_t ntiles, unsigned long long* cursor,
+                         int mode, int grid, cudaStream_t st) {
+    if (ntiles == 0 || nseg <= 0) return cudaSuccess;
+    if (grid < 1) grid = 1;
+    switch (mode) {
+        case MODE_FAST:
+            batch_kernel<MODE_FAST><<<grid, kBatchBlock, 0, st>>>(pool, seg_off, seg_len, tile_prefix, nseg, ntiles, cursor);
+            break;
+        case MODE_SFU_REF:
+            batch_kernel<MODE_SFU_REF><<<grid, kBatchBlock, 0, st>>>(pool, seg_off, seg_len, tile_prefix, nseg, ntiles, cursor);
+            break;
+        case MODE_LIBM_REF:
+            batch_kernel<MODE_LIBM_REF><<<grid, kBatchBlock, 0, st>>>(pool, seg_off, seg_len, tile_prefix, nseg, ntiles, cursor);
+            break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------- error report
+__global__ void __launch_bounds__(256) err_kernel(SoA a, const float* __restrict__ prices,
+                                                  int64_t n, const double* __restrict__ edges,
+                                                  int nb, double rel_floor, ErrAcc* acc) {
+    __shared__ ErrAcc sh[kMaxErrBuckets];
+    __shared__ double sh_edges[kMaxErrBuckets + 1];
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+        sh[i].count = 0;
+        sh[i].max_abs_bits = 0;
+        sh[i].max_rel_bits = 0;
+        sh[i].max_price_bits = 0;
+        sh[i].sum_sq = 0.0;
+    }
+    for (int i = threadIdx.x; i <= nb; i += blockDim.x) sh_edges[i] = edges[i];
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double s = a.s[i], k = a.k[i], r = a.r[i], v = a.v[i], t = a.t[i];
+        const double o = price_fp64(s, k, r, v, t, a.ot[i]);
+        const double d1 = fabs(d1_fp64(s, k, r, v, t));
+        int bk = 0;
+        while (bk < nb - 1 && !(d1 < sh_edges[bk + 1])) ++bk;  // NaN -> last
+        const double err = fabs((double)prices[i] - o);
+        const double den = fabs(o) > rel_floor ? fabs(o) : rel_floor;
+        const double rel = err / den;
+        atomicAdd(&sh[bk].count, 1ull);
+        atomicMax(&sh[bk].max_abs_bits, (unsigned long long)__double_as_longlong(err));
+        atomicMax(&sh[bk].max_rel_bits, (unsigned long long)__double_as_longlong(rel));
+        atomicMax(&sh[bk].max_price_bits, (unsigned long long)__double_as_longlong(fabs(o)));
+        atomicAdd(&sh[bk].sum_sq, err * err);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+        if (sh[i].count == 0) continue;
+        atomicAdd(&acc[i].count, sh[i].count);
+        atomicMax(&acc[i].max_abs_bits, sh[i].max_abs_bits);
+        atomicMax(&acc[i].max_rel_bits, sh[i].max_rel_bits);
+        atomicMax(&acc[i].max_price_bits, sh[i].max_price_bits);
+        atomicAdd(&acc[i].sum_sq, sh[i].sum_sq);
+    }
+}
+
+cudaError_t launch_err_report(const SoA& a, const float* prices, int64_t n,
+                              const double* edges, int nbuckets, double rel_floor,
+                              ErrAcc* acc, int sm_count, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    if (nbuckets < 1 || nbuckets > kMaxErrBuckets) return cudaErrorInvalidValue;
+    int64_t grid = (n + 255) / 256;
+    const int64_t cap = (int64_t)sm_count * 4;
+    if (grid > cap) grid = cap;
+    err_kernel<<<(unsigned)grid, 256, 0, st>>>(a, prices, n, edges, nbuckets, rel_floor, acc);
+    return cudaGetLastError();
+}
+
+// -------------------------------------------------------------- fill (tuning)
+__device__ __forceinline__ float hash_unit(uint64_t x) {
+    x ^= x >> 33; x *= 0xff51afd7ed558ccdull; x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ull; x ^= x >> 33;
+    return (float)(x >> 40) * (1.0f / 16777216.0f);
+}
+
+__global__ void fill_kernel(SoA a, int64_t n, uint32_t seed) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t b = ((uint64_t)seed << 40) ^ ((uint64_t)i * 8);
+        const float s = 10.0f + 190.0f * hash_unit(b + 1);
+        float* ms = const_cast<float*>(a.s);
+        float* mk = const_cast<float*>(a.k);
+        float* mr = const_cast<float*>(a.r);
+        float* mv = const_cast<float*>(a.v);
+        float* mt = const_cast<float*>(a.t);
+        int32_t* mo = const_cast<int32_t*>(a.ot);
+        ms[i] = s;
+        mk[i] = s * (0.5f + hash_unit(b + 2));
+        mr[i] = 0.01f + 0.09f * hash_unit(b + 3);
+        mv[i] = 0.05f + 0.6f * hash_unit(b + 4);
+        mt[i] = 0.05f + 1.95f * hash_unit(b + 5);
+        mo[i] = hash_unit(b + 6) < 0.5f ? 1 : 0;
+    }
+}
+
+cudaError_t launch_fill(const SoA& a, int64_t n, uint32_t seed, int sm_count,
+                        cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    int64_t grid = (n + 255) / 256;
+    const int64_t cap = (int64_t)sm_count * 8;
+    if (grid > cap) grid = cap;
+    fill_kernel<<<(unsigned)grid, 256, 0, st>>>(a, n, seed);
+    return cudaGetLastError();
+}
+
+}  // namespace bsg

@@ -1,0 +1,38 @@
+"""The drop-in CLI: reference argv and file formats, priced on the GPU."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from p3arsec_gb300 import books, build
+
+pytestmark = pytest.mark.gpu
+
+
+def test_cli_round_trip(tmp_path):
+    build.build()
+    book = books.generate(20000, seed=31)
+    fp64 = oracle.price_fp64(book)
+    inp = tmp_path / "in.txt"
+    out = tmp_path / "out.txt"
+    books.write_parsec_input(inp, book, dgrefval=fp64)
+    env = dict(os.environ, BSG_ERR_CHK="1", BSG_NUM_RUNS="5")
+    r = subprocess.run([build.CLI, "8", str(inp), str(out)], stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, text=True, env=env, timeout=120)
+    assert r.returncode == 0, r.stdout
+    assert "Num of Options: 20000" in r.stdout and "Num of Runs: 5" in r.stdout
+    assert "roi.time|" in r.stdout
+    assert "Num Errors: 0" in r.stdout
+    got = books.read_parsec_output(out)
+    assert np.abs(got.astype(np.float64) - fp64).max() <= 1e-4
+
+
+def test_cli_bad_input_exits_1(tmp_path):
+    build.build()
+    bad = tmp_path / "bad.txt"
+    bad.write_text("5\n1 2\n")
+    r = subprocess.run([build.CLI, "1", str(bad), str(tmp_path / "o.txt")],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=60)
+    assert r.returncode == 1 and "ERROR" in r.stdout

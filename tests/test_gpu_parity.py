@@ -1,0 +1,165 @@
+"""GPU parity: the sm_103a kernels, called through the C ABI, against the
+oracle and the reference's golden outputs.
+
+Tolerances (FP32 output):
+  * fast (production) vs the FP64 oracle: max |err| <= 1e-4 on the plain
+    distribution (the spec gate; the reference itself reaches ~8e-5),
+    and <= 2e-4 + 2 ulp(price) on the tails (FP32 cannot resolve 1e-4 above
+    2048; the reference reaches 5e-4 there).
+  * vs the reference's own FP32 prices: <= 2e-4 (both sides ~1e-4 from FP64).
+  * libm_ref (reference operation order, accurate libm) vs the reference:
+    <= 4 ulp of the price, most bit-identical.
+  * FP64 kernel vs the CPU FP64 oracle: rtol 1e-12.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from p3arsec_gb300 import books
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["plain_4096", "tails_4096", "edge"]
+
+
+def ulp(x):
+    return np.spacing(np.abs(x).astype(np.float32)).astype(np.float64)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fast_vs_fp64_and_reference(gpu_ctx, name):
+    book, ref, fp64 = load_golden(name)
+    got = gpu_ctx.price_book(book, num_runs=1, mode="fast").astype(np.float64)
+    err = np.abs(got - fp64)
+    if name == "tails_4096":
+        assert np.all(err <= 2e-4 + 2 * ulp(fp64))
+    else:
+        assert err.max() <= 1e-4, err.max()
+        assert np.abs(got - ref).max() <= 2e-4
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_sfu_ref_close_to_reference(gpu_ctx, name):
+    book, ref, fp64 = load_golden(name)
+    got = gpu_ctx.price_book(book, num_runs=1, mode="sfu_ref").astype(np.float64)
+    tol = 1e-3 if name == "tails_4096" else 5e-4
+    assert np.all(np.abs(got - fp64) <= tol + 4 * ulp(fp64))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_libm_ref_tracks_reference_bits(gpu_ctx, name):
+    book, ref, _ = load_golden(name)
+    got = gpu_ctx.price_book(book, num_runs=1, mode="libm_ref")
+    diff = np.abs(got.astype(np.float64) - ref)
+    assert np.all(diff <= 4 * ulp(ref) + 1e-6)
+    same = np.mean(got.view(np.uint32) == ref.view(np.uint32))
+    assert same > 0.5, same
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp64_kernel_matches_cpu_oracle(gpu_ctx, name):
+    book, _, fp64 = load_golden(name)
+    out = np.empty(len(book), dtype=np.float64)
+    gpu_ctx.price_fp64(*book.arrays(), out)
+    np.testing.assert_allclose(out, fp64, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 7, 8, 9, 31, 127, 128, 129, 1023, 4099, 65537, 100003])
+def test_ragged_sizes_equal_bits_of_a_big_run(gpu_ctx, n):
+    """A prefix priced alone equals the same options priced in a larger call
+    (vector body, ragged tail and scalar paths compute the same bits)."""
+    book = books.generate(131072, seed=11)
+    full = gpu_ctx.price_book(book)
+    part = gpu_ctx.price_book(book.slice(0, n))
+    assert np.array_equal(part.view(np.uint32), full[:n].view(np.uint32))
+
+
+def test_empty_and_zero_runs(gpu_ctx):
+    book = books.generate(0, seed=1)
+    out = np.empty(0, dtype=np.float32)
+    gpu_ctx.price_soa(*book.arrays(), out, n=0, num_runs=100)
+    book = books.generate(10, seed=1)
+    out = np.full(10, -7.0, dtype=np.float32)
+    gpu_ctx.price_soa(*book.arrays(), out, num_runs=0)
+    assert np.all(out == -7.0)
+
+
+def test_num_runs_graph_equals_single_run(gpu_ctx):
+    book = books.generate(300001, seed=12)
+    one = gpu_ctx.price_book(book, num_runs=1)
+    hundred = gpu_ctx.price_book(book, num_runs=100)
+    out = np.empty(len(book), dtype=np.float32)
+    gpu_ctx.price_soa(*book.arrays(), out, num_runs=7, graph=False)
+    assert np.array_equal(one.view(np.uint32), hundred.view(np.uint32))
+    assert np.array_equal(one.view(np.uint32), out.view(np.uint32))
+
+
+def _dev(torch, book, pad=0):
+    arrs = []
+    for a in book.arrays():
+        t = torch.zeros(len(a) + pad, dtype=torch.float32 if a.dtype == np.float32 else torch.int32,
+                        device="cuda:0")
+        t[pad:] = torch.from_numpy(a).cuda()
+        arrs.append(t)
+    return arrs
+
+
+def test_device_pointers_and_misaligned_scalar_path(gpu_ctx):
+    torch = pytest.importorskip("torch")
+    book = books.generate(50001, seed=13)
+    host = gpu_ctx.price_book(book)
+    for pad in (0, 1, 3):
+        d = _dev(torch, book, pad)
+        out = torch.zeros(len(book) + pad, dtype=torch.float32, device="cuda:0")
+        views = [x[pad:] for x in d]
+        gpu_ctx.price_soa(*views, out[pad:], n=len(book), num_runs=2, device=True)
+        torch.cuda.synchronize()
+        got = out[pad:].cpu().numpy()
+        assert np.array_equal(got.view(np.uint32), host.view(np.uint32)), pad
+
+
+def test_all_tunings_give_identical_bits(gpu_ctx):
+    book = books.generate(200003, seed=14)
+    base = gpu_ctx.price_book(book)
+    saved = gpu_ctx.get_tune()
+    try:
+        for lp in (0, 1, 2):
+            for vpt in (1, 2, 4):
+                if lp == 2 and vpt == 4:
+                    continue
+                for block in (128, 256, 512):
+                    for bps in (0, 4):
+                        gpu_ctx.set_tune(vpt, block, bps, lp)
+                        got = gpu_ctx.price_book(book)
+                        assert np.array_equal(got.view(np.uint32), base.view(np.uint32)), (lp, vpt, block, bps)
+    finally:
+        gpu_ctx.set_tune(**saved)
+
+
+def test_out_of_range_device_arguments_are_errors(gpu_ctx):
+    """A size larger than the allocation is refused on the host before any
+    kernel runs; the context stays usable."""
+    torch = pytest.importorskip("torch")
+    from p3arsec_gb300.abi import BsgError
+    book = books.generate(1000, seed=15)
+    d = _dev(torch, book)
+    out = torch.zeros(1000, dtype=torch.float32, device="cuda:0")
+    with pytest.raises(BsgError) as e:
+        gpu_ctx.price_soa(*d, out, n=1001, device=True)
+    assert e.value.status == -1
+    host = np.zeros(4, dtype=np.float32)
+    with pytest.raises(BsgError):
+        gpu_ctx.price_soa(*d, host, n=4, device=True)  # host pointer as device
+    with pytest.raises(BsgError) as e:
+        big = books.generate(gpu_ctx.max_options + 1, seed=1)
+        gpu_ctx.price_book(big)
+    assert e.value.status == -5
+    gpu_ctx.price_soa(*d, out, n=1000, device=True)  # still fine
+
+
+def test_reference_batch_signature(gpu_ctx):
+    from p3arsec_gb300 import BlkSchlsEqEuroNoDiv
+    book, ref, fp64 = load_golden("plain_4096")
+    out = np.zeros(len(book), dtype=np.float32)
+    BlkSchlsEqEuroNoDiv(out, len(book), *book.arrays(), 0.0)
+    assert np.abs(out - fp64).max() <= 1e-4
