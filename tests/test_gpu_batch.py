@@ -75,7 +75,7 @@ def test_batch_rejects_bad_segments(gpu_ctx):
     with pytest.raises(BsgError):
         gpu_ctx.price_batch(pool, out, 1000, [(0, 100), (50, 10)])
     with pytest.raises(BsgError):
-        gpu_ctx.price_batch(pool, out, 2000, [(0, 10)])  # pool larger than allocation
+        gpu_ctx.price_batch(pool, out, 1000 + (1 << 30), [(0, 10)])  # pool past its allocation
     gpu_ctx.price_batch(pool, out, 1000, [(0, 1000)])
 
 
