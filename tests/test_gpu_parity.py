@@ -8,7 +8,7 @@ Tolerances (FP32 output):
     2048; the reference reaches 5e-4 there).
   * vs the reference's own FP32 prices: <= 2e-4 (both sides ~1e-4 from FP64).
   * libm_ref (reference operation order, accurate libm) vs the reference:
-    <= 4 ulp of the price, most bit-identical.
+    <= 5e-5 + 4 ulp of the price, most bit-identical.
   * FP64 kernel vs the CPU FP64 oracle: rtol 1e-12.
 """
 import numpy as np
@@ -51,7 +51,9 @@ def test_libm_ref_tracks_reference_bits(gpu_ctx, name):
     book, ref, _ = load_golden(name)
     got = gpu_ctx.price_book(book, num_runs=1, mode="libm_ref")
     diff = np.abs(got.astype(np.float64) - ref)
-    assert np.all(diff <= 4 * ulp(ref) + 1e-6)
+    # CUDA's expf/logf and glibc's differ by an ulp on some arguments; S (up
+    # to 200) times an ulp of N(d) near 1 gives a few 1e-5
+    assert np.all(diff <= 5e-5 + 4 * ulp(ref)), diff.max()
     same = np.mean(got.view(np.uint32) == ref.view(np.uint32))
     assert same > 0.5, same
 
