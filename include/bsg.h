@@ -130,6 +130,34 @@ int bsg_price_books_plain(bsg_ctx* ctx, const float* sptprice, const float* stri
                           size_t pool_len, const bsg_segment* segs, size_t nseg,
                           int num_runs, unsigned flags);
 
+/* ---- batched books without allocation ----------------------------------
+ * No counterpart in the reference.  For callers that may not allocate
+ * memory (code under a fixed device-memory budget or inside another
+ * runtime's allocator, plugins that must not allocate after start-up,
+ * real-time loops where an allocation can block): the same pricing as
+ * bsg_price_batch with no context and no allocation of any kind.  Its
+ * scratch (segment table, tile prefix, tile counter; 164,104 bytes) is a
+ * fixed device array that every GPU loading this library holds until exit.
+ *  - Runs on the calling thread's current device, on `stream` (a
+ *    cudaStream_t, NULL = legacy default stream).  Pool arrays are device
+ *    memory, 16-byte aligned; segs is a host array.  flags: BSG_DEVICE_PTRS
+ *    is implied; BSG_ASYNC returns once enqueued (keep segs alive until the
+ *    stream reaches the call when it is pinned memory).
+ *  - The first call on a device looks up the scratch array's device address
+ *    (cudaGetSymbolAddress); make that first call before any stream capture.
+ *  - nseg above BSG_NOALLOC_MAX_SEGMENTS returns BSG_ERR_CAPACITY.
+ *  - Every call reuses the same scratch: calls that overlap on the GPU race
+ *    and give wrong prices (never writes outside their own pool).  Serialise
+ *    them on one stream.  Overlapping segments are priced twice (same values).
+ */
+#define BSG_NOALLOC_MAX_SEGMENTS 4096
+
+int bsg_price_batch_noalloc(const float* sptprice, const float* strike,
+                            const float* rate, const float* volatility,
+                            const float* otime, const int32_t* otype, float* prices,
+                            size_t pool_len, const bsg_segment* segs, size_t nseg,
+                            void* stream, unsigned flags);
+
 /* ---- accuracy report ---------------------------------------------------
  * Compares FP32 prices (device) with the FP64 oracle evaluated on the same
  * device inputs, bucketed by |d1| (FP64) against the ascending bucket edges

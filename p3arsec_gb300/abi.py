@@ -79,6 +79,7 @@ SIGNATURES = {
     "bsg_price_fp64": (_I, [_P] + [_P] * 7 + [_SZ, _U]),
     "bsg_price_batch": (_I, [_P] + [_P] * 7 + [_SZ, ctypes.POINTER(Segment), _SZ, _I, _U]),
     "bsg_price_books_plain": (_I, [_P] + [_P] * 7 + [_SZ, ctypes.POINTER(Segment), _SZ, _I, _U]),
+    "bsg_price_batch_noalloc": (_I, [_P] * 7 + [_SZ, ctypes.POINTER(Segment), _SZ, _P, _U]),
     "bsg_error_report": (_I, [_P] + [_P] * 7 + [_SZ, _P, _I, ctypes.c_double, ctypes.POINTER(ErrBucket)]),
     "bsg_autotune": (_I, [_P, _SZ, ctypes.POINTER(Tune)]),
     "bsg_get_tune": (_I, [_P, ctypes.POINTER(Tune)]),
@@ -252,6 +253,22 @@ class Context:
     def set_tune(self, vec_per_thread=1, block=256, blocks_per_sm=0, load_path=0):
         t = Tune(vec_per_thread, block, blocks_per_sm, load_path)
         _check(self.lib, self.h, self.lib.bsg_set_tune(self.h, ctypes.byref(t)))
+
+
+NOALLOC_MAX_SEGMENTS = 4096
+
+
+def price_batch_noalloc(pool, prices, pool_len, segments, stream=0, asynchronous=False):
+    """bsg_price_batch_noalloc: batched books with no allocation (device pool
+    pointers, current device, caller's stream).  Returns the status code."""
+    lib = load()
+    segs = (Segment * max(len(segments), 1))()
+    for i, (o, l) in enumerate(segments):
+        segs[i].offset = int(o)
+        segs[i].len = int(l)
+    flags = DEVICE_PTRS | (ASYNC if asynchronous else 0)
+    return lib.bsg_price_batch_noalloc(*[ptr(x) for x in pool], ptr(prices), pool_len, segs,
+                                       len(segments), stream, flags)
 
 
 def BlkSchlsEqEuroNoDiv(OptionPrice, numOptions, sptprice, strike, rate, volatility,

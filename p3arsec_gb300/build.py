@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-Wall", "-I" + os.path.join(ROOT, "include"),
                      "-I" + CSRC]
-CU_SOURCES = ["bsg_kernels.cu", "bsg_api.cu", "bsg_serve.cu"]
+CU_SOURCES = ["bsg_kernels.cu", "bsg_api.cu", "bsg_serve.cu", "bsg_noalloc.cu"]
 
 
 def nvcc() -> str:
