@@ -177,8 +177,7 @@ def run_ours(args, rank, world, local):
     book = books.generate(n, seed=SEED + rank)
     ctx = Context(local, max_options=n if not args.no_e2e else 1)
     if args.tune:
-        v, bl, bps, lp = (int(x) for x in args.tune.split(","))
-        ctx.set_tune(v, bl, bps, lp)
+        ctx.set_tune(*(int(x) for x in args.tune.split(",")))
         tune = ctx.get_tune()
     else:
         tune = ctx.autotune(n)
@@ -269,6 +268,148 @@ def run_ours(args, rank, world, local):
         dist.destroy_process_group()
 
 
+# ------------------------------------------------------------ batched books
+def book_sizes(nbooks: int, seed: int, lo: int = 1, hi: int = 1 << 20):
+    """Book sizes log-uniform in [lo, hi] (seeded)."""
+    rng = np.random.default_rng(seed)
+    return np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi + 1), nbooks))).astype(np.int64).clip(lo, hi)
+
+
+def run_batch(args, rank, world, local):
+    """Config 4: many uneven books in one pool, one persistent CUDA-graph
+    launch per pass vs one plain launch per book per pass."""
+    import torch
+
+    from p3arsec_gb300 import Context, books
+    from p3arsec_gb300 import build as b
+    b.build()
+    torch.cuda.set_device(local)
+    sizes = book_sizes(args.books, SEED + 4)
+    segs, off = [], 0
+    for nb in sizes:
+        segs.append((off, int(nb)))
+        off += (int(nb) + 63) // 64 * 64  # books start 256-byte aligned
+    pool_len = off
+    total = int(sizes.sum())
+    book = books.generate(pool_len, seed=SEED + 5)
+    dev = [torch.from_numpy(a).to(f"cuda:{local}") for a in book.arrays()]
+    del book
+    out_b = torch.zeros(pool_len, dtype=torch.float32, device=f"cuda:{local}")
+    out_p = torch.zeros(pool_len, dtype=torch.float32, device=f"cuda:{local}")
+    ctx = Context(local, max_options=1)
+    if args.tune:
+        ctx.set_tune(*(int(x) for x in args.tune.split(",")))
+    else:
+        ctx.autotune(1 << 16)  # plain per-book launches are small
+    stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{local}")
+    runs = args.runs
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        l0 = ctx.launches
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local) as clk:
+            e0.record(stream)
+            for _ in range(args.steps):
+                fn()
+            e1.record(stream)
+            e1.synchronize()
+        return e0.elapsed_time(e1) / 1e3, ctx.launches - l0, clk.summary()
+
+    secs_b, launches_b, clk = timed(lambda: ctx.price_batch(dev, out_b, pool_len, segs, num_runs=runs,
+                                                            asynchronous=True))
+    secs_p, launches_p, _ = timed(lambda: ctx.price_batch(dev, out_p, pool_len, segs, num_runs=runs,
+                                                          plain=True, asynchronous=True))
+    torch.cuda.synchronize()
+    same = bool(torch.equal(out_b.view(torch.int32), out_p.view(torch.int32)))
+    value = total * runs * args.steps / secs_b
+    plain = total * runs * args.steps / secs_p
+    peak, peak_src = measured_hbm_peak()
+    achieved = BYTES_PER_OPTION * total * runs * args.steps / secs_b / 1e9
+    line = {
+        "metric": "options/sec (batched books, one persistent launch per pass)", "value": value,
+        "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * secs_b / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded books)",
+        "config": {"workload": f"{args.books} books, sizes log-uniform in [1, 2^20], "
+                               f"{total} options, {runs} passes per step",
+                   "books": args.books, "options": total, "num_runs": runs,
+                   "tune_plain": ctx.get_tune()},
+        "plain_per_book": {"value": plain, "unit": UNIT, "ms_per_step": 1e3 * secs_p / args.steps,
+                           "gpu_launches": launches_p},
+        "speedup_vs_plain": value / plain,
+        "bitwise_equal_to_plain": same,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_src},
+        "gpu_launches": launches_b, "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+# --------------------------------------------------------- precision sweep
+def run_precision(args, rank, world, local):
+    """Config 3: 2^28 options with deep in/out-of-the-money tails; the
+    compensated FP32 path, the reference-order SFU path and the
+    reference-order accurate-libm path against the FP64 oracle kernel, per
+    bucket of |d1|, with the throughput of each."""
+    import torch
+
+    from p3arsec_gb300 import Context, books
+    from p3arsec_gb300 import build as b
+    b.build()
+    torch.cuda.set_device(local)
+    n = args.n
+    book = books.generate(n, seed=SEED + 3, dist="tails")
+    dev = [torch.from_numpy(a).to(f"cuda:{local}") for a in book.arrays()]
+    del book
+    out = torch.empty(n, dtype=torch.float32, device=f"cuda:{local}")
+    ctx = Context(local, max_options=1)
+    if args.tune:
+        ctx.set_tune(*(int(x) for x in args.tune.split(",")))
+    else:
+        ctx.autotune(n)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{local}")
+    edges = np.array([0.0, 0.5, 1.0, 2.0, 3.0, 4.0, 5.0, 6.0, 8.0, 12.0, np.inf])
+    res = {}
+    for mode in ("fast", "sfu_ref", "libm_ref"):
+        def step():
+            ctx.price_soa(*dev, out, n=n, num_runs=args.runs, mode=mode, device=True,
+                          asynchronous=True)
+        for _ in range(args.warmup):
+            step()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        e1.synchronize()
+        secs = e0.elapsed_time(e1) / 1e3
+        rep = ctx.error_report(dev, out, n, edges, rel_floor=1e-3)
+        res[mode] = {"options_per_s": n * args.runs * args.steps / secs,
+                     "max_abs": max(x["max_abs"] for x in rep),
+                     "rms_abs": (sum(x["sum_sq_abs"] for x in rep) / n) ** 0.5,
+                     "buckets": [{"d1": [x["d1_lo"], x["d1_hi"]], "count": x["count"],
+                                  "max_abs": x["max_abs"], "rms_abs": x["rms_abs"],
+                                  "max_rel": x["max_rel"], "max_price": x["max_price"]}
+                                 for x in rep]}
+    line = {"metric": "precision sweep: max/RMS error vs FP64 per |d1| bucket",
+            "value": res["fast"]["options_per_s"], "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic (seeded, K=S*U[0.05,20], t~U[0.001,5])",
+            "config": {"workload": f"precision sweep, {n} options, tails distribution",
+                       "options": n, "num_runs": args.runs, "rel_floor": 1e-3},
+            "modes": res}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 # ---------------------------------------------------------- reference arm
 def run_reference(args, rank, world, local):
     """The reference's CPU path (the oracle port of its FastFlow map: same
@@ -313,20 +454,25 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=["map"], default="map")
+    ap.add_argument("--config", choices=["map", "batch", "precision"], default="map")
+    ap.add_argument("--books", type=int, default=4096, help="batch config: number of books")
     ap.add_argument("--n", type=int, default=N_OPTIONS)
     ap.add_argument("--runs", type=int, default=NUM_RUNS)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 error report")
     ap.add_argument("--tune", default=None,
-                    help="vec_per_thread,block,blocks_per_sm,load_path instead of autotuning")
+                    help="vec_per_thread,block,blocks_per_sm,load_path[,pdl] instead of autotuning")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world, local)
+    elif args.config == "batch":
+        run_batch(args, rank, world, local)
+    elif args.config == "precision":
+        run_precision(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 

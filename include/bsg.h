@@ -190,7 +190,9 @@ typedef struct bsg_tune {
     int vec_per_thread; /* float4 groups per thread per tile: 1, 2 or 4 */
     int block;          /* threads per block: 128, 256 or 512 */
     int blocks_per_sm;  /* grid = blocks_per_sm * SM count; 0 = one block per tile */
-    int load_path;      /* 0 = LDG.128 non-coherent, 1 = LDG.128 evict-first */
+    int load_path;      /* 0 = LDG.128 non-coherent, 1 = LDG.128 evict-first,
+                           2 = LDG.256 non-coherent (8 options per load) */
+    int pdl;            /* 1 = programmatic dependent launch between passes */
 } bsg_tune;
 
 int bsg_autotune(bsg_ctx* ctx, size_t n, bsg_tune* out);

@@ -71,7 +71,7 @@ struct bsg_ctx {
     size_t cap = 0;     // max_options
     size_t cap_al = 0;  // per-array stride in the resident buffer
     char* dev_buf = nullptr;
-    bsg::MapCfg tune{1, 256, 0, 0};
+    bsg::MapCfg tune{1, 256, 0, 0, 0};
     std::mutex mu;
     std::string err;
     uint64_t launches = 0;
@@ -679,6 +679,7 @@ int bsg_get_tune(const bsg_ctx* c, bsg_tune* out) {
     out->block = c->tune.block;
     out->blocks_per_sm = c->tune.blocks_per_sm;
     out->load_path = c->tune.load_path;
+    out->pdl = c->tune.pdl;
     return BSG_OK;
 }
 
@@ -687,14 +688,14 @@ static bool tune_valid(const bsg_tune* t) {
                         (t->vec_per_thread == 4 && t->load_path != 2);
     const bool blk_ok = t->block == 128 || t->block == 256 || t->block == 512;
     return vpt_ok && blk_ok && t->blocks_per_sm >= 0 && t->blocks_per_sm <= 64 &&
-           t->load_path >= 0 && t->load_path <= 2;
+           t->load_path >= 0 && t->load_path <= 2 && (t->pdl == 0 || t->pdl == 1);
 }
 
 int bsg_set_tune(bsg_ctx* c, const bsg_tune* t) {
     if (!c || !t) return BSG_ERR_INVALID_ARG;
     std::lock_guard<std::mutex> lk(c->mu);
     if (!tune_valid(t)) return fail(c, BSG_ERR_INVALID_ARG, "unsupported tuning");
-    c->tune = bsg::MapCfg{t->vec_per_thread, t->block, t->blocks_per_sm, t->load_path};
+    c->tune = bsg::MapCfg{t->vec_per_thread, t->block, t->blocks_per_sm, t->load_path, t->pdl};
     return BSG_OK;
 }
 
@@ -724,8 +725,8 @@ static bool tune_cache_lookup(const std::string& key, bsg_tune* t) {
         const size_t bar = line.rfind('|');
         if (bar == std::string::npos || line.compare(0, bar, key) != 0) continue;
         bsg_tune x;
-        if (std::sscanf(line.c_str() + bar + 1, "%d %d %d %d", &x.vec_per_thread, &x.block,
-                        &x.blocks_per_sm, &x.load_path) == 4 && tune_valid(&x)) {
+        if (std::sscanf(line.c_str() + bar + 1, "%d %d %d %d %d", &x.vec_per_thread, &x.block,
+                        &x.blocks_per_sm, &x.load_path, &x.pdl) == 5 && tune_valid(&x)) {
             *t = x;
             found = true;
         }
@@ -738,7 +739,7 @@ static void tune_cache_store(const std::string& key, const bsg_tune& t) {
     if (!path || !*path) return;
     std::ofstream f(path, std::ios::app);
     f << key << "|" << t.vec_per_thread << " " << t.block << " " << t.blocks_per_sm << " "
-      << t.load_path << "\n";
+      << t.load_path << " " << t.pdl << "\n";
 }
 
 extern "C" int bsg_autotune(bsg_ctx* c, size_t n, bsg_tune* out) {
@@ -748,7 +749,7 @@ extern "C" int bsg_autotune(bsg_ctx* c, size_t n, bsg_tune* out) {
     const std::string key = tune_key(c, n);
     bsg_tune best{};
     if (tune_cache_lookup(key, &best)) {
-        c->tune = bsg::MapCfg{best.vec_per_thread, best.block, best.blocks_per_sm, best.load_path};
+        c->tune = bsg::MapCfg{best.vec_per_thread, best.block, best.blocks_per_sm, best.load_path, best.pdl};
         if (out) *out = best;
         return BSG_OK;
     }
@@ -772,14 +773,15 @@ extern "C" int bsg_autotune(bsg_ctx* c, size_t n, bsg_tune* out) {
     BSG_CK(c, cudaEventCreate(&e0));
     BSG_CK(c, cudaEventCreate(&e1));
     float best_ms = 1e30f;
-    const int reps = 3;
+    const int reps = 5;  // back to back, as the NUM_RUNS passes run
     for (int lp = 0; lp <= 2; ++lp)
         for (int vpt : {1, 2, 4})
             for (int block : {128, 256, 512})
-                for (int bps : {0, 2, 4, 8}) {
-                    bsg_tune t{vpt, block, bps, lp};
+                for (int bps : {0, 2, 4, 8})
+                for (int pdl : {0, 1}) {
+                    bsg_tune t{vpt, block, bps, lp, pdl};
                     if (!tune_valid(&t)) continue;
-                    const bsg::MapCfg cfg{vpt, block, bps, lp};
+                    const bsg::MapCfg cfg{vpt, block, bps, lp, pdl};
                     e = bsg::launch_map(a, (int64_t)n, bsg::MODE_FAST, cfg, c->sm_count, c->stream);
                     if (e != cudaSuccess) break;
                     cudaEventRecord(e0, c->stream);
@@ -800,7 +802,7 @@ extern "C" int bsg_autotune(bsg_ctx* c, size_t n, bsg_tune* out) {
     cudaEventDestroy(e1);
     if (e != cudaSuccess) return cuda_fail(c, e, "autotune launch");
     BSG_CK(c, cudaStreamSynchronize(c->stream));
-    c->tune = bsg::MapCfg{best.vec_per_thread, best.block, best.blocks_per_sm, best.load_path};
+    c->tune = bsg::MapCfg{best.vec_per_thread, best.block, best.blocks_per_sm, best.load_path, best.pdl};
     tune_cache_store(key, best);
     if (out) *out = best;
     return BSG_OK;

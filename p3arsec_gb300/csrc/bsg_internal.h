@@ -26,6 +26,7 @@ struct MapCfg {
     int block;         // threads per block
     int blocks_per_sm; // 0: one block per tile; else grid = blocks_per_sm * SMs
     int load_path;     // 0: v4 nc; 1: v4 + L2 evict_first; 2: v8 (256-bit) nc
+    int pdl;           // 1: launch with programmatic stream serialization
 };
 
 // Accumulators of one error bucket (device scratch, zeroed per report).

@@ -117,8 +117,21 @@ __device__ __forceinline__ void price_groups(const SoA& a, int64_t g0, int64_t g
 // Vector kernel: options [0, n - n % W) in groups of W; the last n % W
 // options by block 0.  blocks_per_sm == 0: each block prices one tile of
 // blockDim.x * VPT groups; otherwise blocks stride over tiles.
+// Programmatic dependent launch: every block lets the next pass launch as
+// soon as it starts (the next pass reads only the inputs, which no pass
+// writes), and waits for the previous pass to complete only after its own
+// stores, so a pass still completes after the one before it.  Both
+// instructions are no-ops for a launch without the PDL attribute.
+__device__ __forceinline__ void pdl_trigger() {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 template <int M, int W, int VPT, int LP>
 __global__ void __launch_bounds__(512) map_vec_kernel(SoA a, int64_t n) {
+    pdl_trigger();
     const unsigned long long pol = (LP == 1) ? evict_first_policy() : 0ull;
     const int64_t ngroups = n / W;
     const int64_t tile = (int64_t)blockDim.x * VPT;
@@ -130,6 +143,7 @@ __global__ void __launch_bounds__(512) map_vec_kernel(SoA a, int64_t n) {
         const int64_t i = ngroups * W + threadIdx.x;
         if (i < n) price_scalar<M>(a, i);
     }
+    pdl_wait();
 }
 
 // Scalar kernel: any 4-byte aligned pointers.
@@ -176,7 +190,18 @@ static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg,
     if (grid < 1) grid = 1;
     const dim3 g((unsigned)grid), b((unsigned)block);
 
-#define BSG_LAUNCH(W_, V_, L_) map_vec_kernel<M, W_, V_, L_><<<g, b, 0, st>>>(a, n)
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = g;
+    lc.blockDim = b;
+    lc.dynamicSmemBytes = 0;
+    lc.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    lc.attrs = attr;
+    lc.numAttrs = cfg.pdl ? 1 : 0;
+    cudaError_t le = cudaSuccess;
+#define BSG_LAUNCH(W_, V_, L_) le = cudaLaunchKernelEx(&lc, map_vec_kernel<M, W_, V_, L_>, a, n)
     if constexpr (M == MODE_FAST) {
         switch (cfg.load_path * 10 + cfg.vpt) {
             case 1: BSG_LAUNCH(4, 1, 0); break;
@@ -195,6 +220,7 @@ static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg,
         else BSG_LAUNCH(4, 1, 0);
     }
 #undef BSG_LAUNCH
+    if (le != cudaSuccess) return le;
     return cudaGetLastError();
 }
 

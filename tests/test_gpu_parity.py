@@ -130,10 +130,10 @@ def test_all_tunings_give_identical_bits(gpu_ctx):
                 if lp == 2 and vpt == 4:
                     continue
                 for block in (128, 256, 512):
-                    for bps in (0, 4):
-                        gpu_ctx.set_tune(vpt, block, bps, lp)
-                        got = gpu_ctx.price_book(book)
-                        assert np.array_equal(got.view(np.uint32), base.view(np.uint32)), (lp, vpt, block, bps)
+                    for bps, pdl in ((0, 0), (4, 0), (0, 1), (4, 1)):
+                        gpu_ctx.set_tune(vpt, block, bps, lp, pdl)
+                        got = gpu_ctx.price_book(book, num_runs=3)
+                        assert np.array_equal(got.view(np.uint32), base.view(np.uint32)), (lp, vpt, block, bps, pdl)
     finally:
         gpu_ctx.set_tune(**saved)
 
