@@ -180,6 +180,109 @@ int bsg_error_report(bsg_ctx* ctx, const float* sptprice, const float* strike,
                      const float* prices, size_t n, const double* edges,
                      int nbuckets, double rel_floor, bsg_err_bucket* out);
 
+/* ---- serving -----------------------------------------------------------
+ * A request loop that admits pricing requests of any size while others are
+ * on the GPU.  Admission is by a device-memory budget: a request holds 28
+ * bytes per option of a resident device pool from admission to completion,
+ * and waits in FIFO order while the pool or every batch slot is busy.  All
+ * requests admitted since the last launch are coalesced into one batch: one
+ * kernel gathers their inputs from pinned host memory into the pool, the
+ * persistent batch kernel prices them, one kernel writes the prices back to
+ * each request's host output.  Up to max_inflight batches overlap on the
+ * GPU (one stream each).  With plain = 1 the loop instead prices one request
+ * at a time with per-array copies and one plain map launch (the baseline).
+ * Request arrays are host memory; pinned memory (bsg_host_alloc or
+ * cudaHostRegister) is required for the batched path and recommended for the
+ * plain path.  A request's result is bit-identical alone and in any mix. */
+typedef struct bsg_server bsg_server;
+
+typedef struct bsg_server_config {
+    int device;
+    size_t budget_bytes;      /* device pool for admitted requests (28 B/option) */
+    int max_inflight;         /* batches on the GPU at once, 1..16 */
+    size_t max_batch_options; /* cap per batch (0 = the whole pool) */
+    int max_batch_requests;   /* cap per batch, 1..65536 (0 = 4096) */
+    int plain;                /* 1 = one plain launch per request, serially */
+    unsigned flags;           /* BSG_MODE_* */
+    double batch_timeout_s;   /* bound on waiting for one batch (0 = 30 s) */
+} bsg_server_config;
+
+typedef struct bsg_request {
+    const float* sptprice;
+    const float* strike;
+    const float* rate;
+    const float* volatility;
+    const float* otime;
+    const int32_t* otype;
+    float* prices;
+    size_t n;
+} bsg_request;
+
+typedef struct bsg_server_stats {
+    uint64_t submitted, completed, cancelled, failed;
+    uint64_t batches, kernel_launches, options_priced;
+    uint64_t max_batch_requests_seen;
+    uint64_t queued, inflight_requests;
+} bsg_server_stats;
+
+int bsg_server_create(bsg_server** out, const bsg_server_config* cfg);
+/* Destroys the loop: queued requests are cancelled, in-flight ones finish. */
+void bsg_server_destroy(bsg_server* srv);
+/* Registers host memory [ptr, ptr + bytes) for request arrays of the batched
+ * path (pins it with cudaHostRegister unless it is already pinned).  Every
+ * array of a batched request must lie inside one registered range: the GPU
+ * reads inputs and writes prices there directly over the host link. */
+int bsg_server_register(bsg_server* srv, void* ptr, size_t bytes);
+/* Enqueues a request (non-blocking).  BSG_ERR_BUDGET if it can never fit. */
+int bsg_server_submit(bsg_server* srv, const bsg_request* req, uint64_t* id);
+/* Waits up to timeout_s (< 0: no limit) for request id.  Returns its final
+ * status (BSG_OK priced, BSG_ERR_CANCELLED, BSG_ERR_TIMEOUT for a batch that
+ * overran batch_timeout_s, ...) and releases it, or BSG_ERR_TIMEOUT while it
+ * is still pending (it stays pending).  latency_s (optional): submit to
+ * completion. */
+int bsg_server_wait(bsg_server* srv, uint64_t id, double timeout_s, double* latency_s);
+/* Cancels a request that is still queued; BSG_ERR_STATE once admitted. */
+int bsg_server_cancel(bsg_server* srv, uint64_t id);
+/* Holds (1) or resumes (0) admission; queued requests stay queued. */
+int bsg_server_pause(bsg_server* srv, int paused);
+int bsg_server_get_stats(bsg_server* srv, bsg_server_stats* out);
+
+/* Open-loop trace: Poisson arrivals at rate_per_s for duration_s, request
+ * sizes log-uniform in [min_n, max_n], each request a slice of the caller's
+ * pinned host pool (5 float arrays + otype, and a prices array, each of
+ * pool_n options) at a seeded offset.  Latency runs from each request's
+ * scheduled arrival to its completion.  Latencies of completed requests are
+ * written to latencies_out (capacity latencies_cap; may be NULL). */
+typedef struct bsg_trace_config {
+    double rate_per_s;
+    double duration_s;
+    size_t min_n, max_n;
+    uint64_t seed;
+    const float* sptprice;
+    const float* strike;
+    const float* rate;
+    const float* volatility;
+    const float* otime;
+    const int32_t* otype;
+    float* prices;
+    size_t pool_n;
+    double drain_timeout_s; /* bound on waiting for the last requests (0 = 60 s) */
+} bsg_trace_config;
+
+typedef struct bsg_trace_result {
+    uint64_t requests, completed, failed;
+    uint64_t options;
+    double wall_s;          /* first arrival to last completion */
+    double options_per_s, requests_per_s;
+    double p50_s, p99_s, p999_s, max_s, mean_s;
+    double mean_batch_requests;
+    uint64_t batches;
+    double late_submit_max_s; /* how far behind schedule the submitter fell */
+} bsg_trace_result;
+
+int bsg_serve_trace(const bsg_server_config* cfg, const bsg_trace_config* trace,
+                    bsg_trace_result* out, double* latencies_out, size_t latencies_cap);
+
 /* ---- tuning ------------------------------------------------------------
  * The plain map is a family of kernels: vector width per thread, block size
  * and grid size.  bsg_autotune times the candidates on the context's device

@@ -61,6 +61,54 @@ class Tune(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("budget_bytes", ctypes.c_size_t),
+                ("max_inflight", ctypes.c_int), ("max_batch_options", ctypes.c_size_t),
+                ("max_batch_requests", ctypes.c_int), ("plain", ctypes.c_int),
+                ("flags", ctypes.c_uint), ("batch_timeout_s", ctypes.c_double)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("sptprice", ctypes.c_void_p), ("strike", ctypes.c_void_p),
+                ("rate", ctypes.c_void_p), ("volatility", ctypes.c_void_p),
+                ("otime", ctypes.c_void_p), ("otype", ctypes.c_void_p),
+                ("prices", ctypes.c_void_p), ("n", ctypes.c_size_t)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_uint64) for f in (
+        "submitted", "completed", "cancelled", "failed", "batches", "kernel_launches",
+        "options_priced", "max_batch_requests_seen", "queued", "inflight_requests")]
+
+    def as_dict(self):
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
+
+
+class TraceConfig(ctypes.Structure):
+    _fields_ = [("rate_per_s", ctypes.c_double), ("duration_s", ctypes.c_double),
+                ("min_n", ctypes.c_size_t), ("max_n", ctypes.c_size_t),
+                ("seed", ctypes.c_uint64),
+                ("sptprice", ctypes.c_void_p), ("strike", ctypes.c_void_p),
+                ("rate", ctypes.c_void_p), ("volatility", ctypes.c_void_p),
+                ("otime", ctypes.c_void_p), ("otype", ctypes.c_void_p),
+                ("prices", ctypes.c_void_p), ("pool_n", ctypes.c_size_t),
+                ("drain_timeout_s", ctypes.c_double)]
+
+
+class TraceResult(ctypes.Structure):
+    _fields_ = [("requests", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+                ("failed", ctypes.c_uint64), ("options", ctypes.c_uint64),
+                ("wall_s", ctypes.c_double), ("options_per_s", ctypes.c_double),
+                ("requests_per_s", ctypes.c_double), ("p50_s", ctypes.c_double),
+                ("p99_s", ctypes.c_double), ("p999_s", ctypes.c_double),
+                ("max_s", ctypes.c_double), ("mean_s", ctypes.c_double),
+                ("mean_batch_requests", ctypes.c_double), ("batches", ctypes.c_uint64),
+                ("late_submit_max_s", ctypes.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 # Every symbol the header declares, with its ctypes signature.
 _P = ctypes.c_void_p
 _SZ = ctypes.c_size_t
@@ -82,6 +130,16 @@ SIGNATURES = {
     "bsg_price_books_plain": (_I, [_P] + [_P] * 7 + [_SZ, ctypes.POINTER(Segment), _SZ, _I, _U]),
     "bsg_price_batch_noalloc": (_I, [_P] * 7 + [_SZ, ctypes.POINTER(Segment), _SZ, _P, _U]),
     "bsg_error_report": (_I, [_P] + [_P] * 7 + [_SZ, _P, _I, ctypes.c_double, ctypes.POINTER(ErrBucket)]),
+    "bsg_server_create": (_I, [ctypes.POINTER(_P), ctypes.POINTER(ServerConfig)]),
+    "bsg_server_destroy": (None, [_P]),
+    "bsg_server_register": (_I, [_P, _P, _SZ]),
+    "bsg_server_submit": (_I, [_P, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]),
+    "bsg_server_wait": (_I, [_P, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+    "bsg_server_cancel": (_I, [_P, ctypes.c_uint64]),
+    "bsg_server_pause": (_I, [_P, _I]),
+    "bsg_server_get_stats": (_I, [_P, ctypes.POINTER(ServerStats)]),
+    "bsg_serve_trace": (_I, [ctypes.POINTER(ServerConfig), ctypes.POINTER(TraceConfig),
+                             ctypes.POINTER(TraceResult), _P, _SZ]),
     "bsg_autotune": (_I, [_P, _SZ, ctypes.POINTER(Tune)]),
     "bsg_get_tune": (_I, [_P, ctypes.POINTER(Tune)]),
     "bsg_set_tune": (_I, [_P, ctypes.POINTER(Tune)]),
@@ -254,6 +312,86 @@ class Context:
     def set_tune(self, vec_per_thread=1, block=256, blocks_per_sm=0, load_path=0, pdl=0):
         t = Tune(vec_per_thread, block, blocks_per_sm, load_path, pdl)
         _check(self.lib, self.h, self.lib.bsg_set_tune(self.h, ctypes.byref(t)))
+
+
+class Server:
+    """bsg_server: the continuous-batching request loop (see include/bsg.h)."""
+
+    def __init__(self, device=0, budget_bytes=64 << 30, max_inflight=4, max_batch_options=0,
+                 max_batch_requests=0, plain=False, mode="fast", batch_timeout_s=30.0):
+        self.lib = load()
+        self.cfg = ServerConfig(device, budget_bytes, max_inflight, max_batch_options,
+                                max_batch_requests, 1 if plain else 0, MODES[mode],
+                                batch_timeout_s)
+        h = _P()
+        st = self.lib.bsg_server_create(ctypes.byref(h), ctypes.byref(self.cfg))
+        if st != 0:
+            raise BsgError(st, self.lib.bsg_strerror(st).decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.bsg_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def register(self, arr):
+        """Pin/register a host array (numpy) for batched requests."""
+        st = self.lib.bsg_server_register(self.h, ptr(arr), arr.nbytes)
+        if st != 0:
+            raise BsgError(st, self.lib.bsg_strerror(st).decode())
+
+    def submit(self, s, k, r, v, t, otype, prices, n=None) -> int:
+        if n is None:
+            n = len(s)
+        req = Request(ptr(s), ptr(k), ptr(r), ptr(v), ptr(t), ptr(otype), ptr(prices), n)
+        rid = ctypes.c_uint64()
+        st = self.lib.bsg_server_submit(self.h, ctypes.byref(req), ctypes.byref(rid))
+        if st != 0:
+            raise BsgError(st, self.lib.bsg_strerror(st).decode())
+        return int(rid.value)
+
+    def wait(self, rid: int, timeout_s: float = -1.0):
+        """Returns (status, latency_s); status BSG_ERR_TIMEOUT leaves it pending."""
+        lat = ctypes.c_double(float("nan"))
+        st = self.lib.bsg_server_wait(self.h, rid, timeout_s, ctypes.byref(lat))
+        return st, lat.value
+
+    def cancel(self, rid: int) -> int:
+        return self.lib.bsg_server_cancel(self.h, rid)
+
+    def pause(self, paused: bool = True):
+        self.lib.bsg_server_pause(self.h, 1 if paused else 0)
+
+    def stats(self) -> dict:
+        x = ServerStats()
+        self.lib.bsg_server_get_stats(self.h, ctypes.byref(x))
+        return x.as_dict()
+
+
+def serve_trace(host_pool, prices, rate_per_s, duration_s, min_n=16, max_n=1 << 20, seed=1,
+                device=0, budget_bytes=64 << 30, max_inflight=4, plain=False, mode="fast",
+                max_batch_options=0, max_batch_requests=0, drain_timeout_s=60.0,
+                latencies=None):
+    """bsg_serve_trace over a host pool (6 arrays) and a prices array."""
+    lib = load()
+    cfg = ServerConfig(device, budget_bytes, max_inflight, max_batch_options, max_batch_requests,
+                       1 if plain else 0, MODES[mode], 30.0)
+    n = len(host_pool[0])
+    tc = TraceConfig(rate_per_s, duration_s, min_n, max_n, seed, *[ptr(a) for a in host_pool],
+                     ptr(prices), n, drain_timeout_s)
+    res = TraceResult()
+    cap = 0 if latencies is None else len(latencies)
+    st = lib.bsg_serve_trace(ctypes.byref(cfg), ctypes.byref(tc), ctypes.byref(res),
+                             ptr(latencies) if latencies is not None else None, cap)
+    if st != 0:
+        raise BsgError(st, lib.bsg_strerror(st).decode())
+    return res.as_dict()
 
 
 NOALLOC_MAX_SEGMENTS = 4096

@@ -1,0 +1,814 @@
+// bsg_serve.cu -- the request loop: continuous batching of pricing requests.
+//
+// Threads:
+//  * callers submit requests (bsg_server_submit) into a FIFO queue;
+//  * the dispatcher admits queued requests while the device pool (the
+//    memory budget) and a batch slot are free, coalesces everything admitted
+//    into one batch and enqueues it on the slot's stream;
+//  * the completer waits (bounded, polling cudaEventQuery) for batches in
+//    launch order, frees their pool ranges and completes their requests.
+// Up to max_inflight batches are on the GPU at once, so requests arriving
+// while a batch runs are admitted into the next one and their transfers and
+// pricing overlap the running batch.
+//
+// Batched path, per batch: one table upload, an ingest kernel that gathers
+// every request's inputs from registered (pinned) host memory into the pool,
+// the persistent batch kernel over the requests' pool segments, and an
+// egress kernel that writes the prices to each request's host output.  No
+// per-request copy calls.  Plain path (plain = 1): one request at a time,
+// six host-to-device copies, one plain map launch, one device-to-host copy.
+#include "bsg.h"
+#include "bsg_internal.h"
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <new>
+#include <random>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+namespace {
+
+constexpr uint64_t kTile = 8192;   // options per ingest/egress/batch tile
+constexpr uint64_t kAlign = 64;    // pool ranges start 256-byte aligned
+constexpr int kThreads = 256;
+
+double now_s() {
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+// One request of a batch as the ingest/egress kernels see it.  Host arrays
+// are given by their device-usable addresses.
+struct Desc {
+    const float* src[5];
+    const int32_t* ot;
+    float* out;
+    uint64_t off;  // pool offset in options
+    uint64_t n;
+};
+
+__device__ __forceinline__ int find_segment(const uint64_t* pre, int m, uint64_t tile) {
+    int lo = 0, hi = m - 1;
+    while (lo < hi) {  // largest request whose first tile <= tile
+        const int mid = (lo + hi + 1) >> 1;
+        if (pre[mid] <= tile) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Host -> pool: 6 arrays of every request, tile by tile.
+__global__ void __launch_bounds__(kThreads) ingest_kernel(const Desc* __restrict__ d,
+                                                          const uint64_t* __restrict__ pre, int m,
+                                                          uint64_t ntiles, bsg::SoA pool) {
+    __shared__ int sh_q;
+    float* ps = const_cast<float*>(pool.s);
+    float* pk = const_cast<float*>(pool.k);
+    float* pr = const_cast<float*>(pool.r);
+    float* pv = const_cast<float*>(pool.v);
+    float* pt = const_cast<float*>(pool.t);
+    int32_t* po = const_cast<int32_t*>(pool.ot);
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        if (threadIdx.x == 0) sh_q = find_segment(pre, m, tile);
+        __syncthreads();
+        const Desc q = d[sh_q];
+        const uint64_t b = (tile - pre[sh_q]) * kTile;
+        const uint64_t e = (b + kTile < q.n) ? b + kTile : q.n;
+        for (uint64_t i = b + threadIdx.x; i < e; i += kThreads) {
+            const uint64_t o = q.off + i;
+            ps[o] = q.src[0][i];
+            pk[o] = q.src[1][i];
+            pr[o] = q.src[2][i];
+            pv[o] = q.src[3][i];
+            pt[o] = q.src[4][i];
+            po[o] = q.ot[i];
+        }
+        __syncthreads();
+    }
+}
+
+// Pool prices -> each request's host output.
+__global__ void __launch_bounds__(kThreads) egress_kernel(const Desc* __restrict__ d,
+                                                          const uint64_t* __restrict__ pre, int m,
+                                                          uint64_t ntiles,
+                                                          const float* __restrict__ pool_out) {
+    __shared__ int sh_q;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        if (threadIdx.x == 0) sh_q = find_segment(pre, m, tile);
+        __syncthreads();
+        const Desc q = d[sh_q];
+        const uint64_t b = (tile - pre[sh_q]) * kTile;
+        const uint64_t e = (b + kTile < q.n) ? b + kTile : q.n;
+        for (uint64_t i = b + threadIdx.x; i < e; i += kThreads) q.out[i] = pool_out[q.off + i];
+        __syncthreads();
+    }
+}
+
+enum State { Q_QUEUED, Q_ADMITTED, Q_DONE };
+
+struct Request {
+    uint64_t id;
+    bsg_request r;
+    uint64_t span;  // pool options held (n rounded up to kAlign)
+    uint64_t off;
+    double t_ref;   // latency reference: submit time or scheduled arrival
+    double t_done;
+    State state;
+    int status;
+    bool auto_release;
+    double* lat_slot;
+    Desc desc;
+};
+
+struct Slot {
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    char* h_tab = nullptr;  // pinned table block
+    char* d_tab = nullptr;  // device table block
+    unsigned long long* d_cursor = nullptr;
+    std::vector<Request*> reqs;
+    bool busy = false;
+};
+
+struct HostRange {
+    uintptr_t b, e;
+    intptr_t delta;  // device address = host address + delta
+    bool owned;      // registered by us (unregister at destroy)
+};
+
+// The driver's record of the CUDA allocation or registration containing p
+// (cuPointerGetAttribute RANGE_START_ADDR / RANGE_SIZE), resolved at run time.
+typedef CUresult (*PtrAttrFn)(void*, CUpointer_attribute, CUdeviceptr);
+
+bool cuda_range(const void* p, uintptr_t* b, size_t* sz) {
+    static PtrAttrFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &f, 12000,
+                                             cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            f = nullptr;
+        }
+        return reinterpret_cast<PtrAttrFn>(f);
+    }();
+    if (!fn) return false;
+    CUdeviceptr start = 0;
+    size_t size = 0;
+    if (fn(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, (CUdeviceptr)p) != CUDA_SUCCESS ||
+        fn(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, (CUdeviceptr)p) != CUDA_SUCCESS)
+        return false;
+    *b = (uintptr_t)start;
+    *sz = size;
+    return true;
+}
+
+size_t table_bytes(int cap) {
+    return (size_t)cap * sizeof(Desc) + (3 * (size_t)cap + 1) * sizeof(uint64_t);
+}
+
+}  // namespace
+
+struct bsg_server {
+    bsg_server_config cfg{};
+    int device = 0, sm_count = 0, batch_grid = 1, mode = 0, max_req = 4096;
+    double batch_timeout = 30.0;
+    char* d_pool = nullptr;
+    uint64_t cap = 0;  // options
+    bsg::SoA pool{};
+    std::map<uint64_t, uint64_t> free_list;  // start -> length (options)
+    std::vector<Slot> slots;
+    std::vector<HostRange> hosts;
+    std::mutex mu;
+    std::condition_variable cv_disp, cv_comp, cv_done;
+    std::deque<Request*> queue;
+    std::deque<int> inflight;
+    std::unordered_map<uint64_t, Request*> reqs;
+    std::thread disp, comp;
+    bool stop = false, paused = false;
+    uint64_t next_id = 1, free_gen = 0;
+    bsg_server_stats st{};
+
+    // ------------------------------------------------------------ pool
+    bool pool_alloc(uint64_t span, uint64_t* off) {
+        for (auto it = free_list.begin(); it != free_list.end(); ++it) {
+            if (it->second >= span) {
+                *off = it->first;
+                const uint64_t rest = it->second - span;
+                const uint64_t start = it->first + span;
+                free_list.erase(it);
+                if (rest) free_list[start] = rest;
+                return true;
+            }
+        }
+        return false;
+    }
+    void pool_free(uint64_t off, uint64_t span) {
+        auto it = free_list.emplace(off, span).first;
+        auto nx = std::next(it);
+        if (nx != free_list.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_list.erase(nx);
+        }
+        if (it != free_list.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_list.erase(it);
+            }
+        }
+    }
+
+    const HostRange* host_range(const void* p, size_t bytes) const {
+        const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+        for (const auto& h : hosts)
+            if (a >= h.b && a + bytes <= h.e && a + bytes >= a) return &h;
+        return nullptr;
+    }
+
+    int free_slot() const {
+        for (size_t i = 0; i < slots.size(); ++i)
+            if (!slots[i].busy) return (int)i;
+        return -1;
+    }
+
+    // --------------------------------------------------------- enqueue
+    int enqueue_batched(Slot& sl) {
+        const int m = (int)sl.reqs.size();
+        Desc* hd = reinterpret_cast<Desc*>(sl.h_tab);
+        uint64_t* hoff = reinterpret_cast<uint64_t*>(sl.h_tab + (size_t)m * sizeof(Desc));
+        uint64_t* hlen = hoff + m;
+        uint64_t* hpre = hlen + m;
+        uint64_t acc = 0;
+        for (int i = 0; i < m; ++i) {
+            const Request* q = sl.reqs[i];
+            hd[i] = q->desc;
+            hoff[i] = q->off;
+            hlen[i] = q->r.n;
+            hpre[i] = acc;
+            acc += (q->r.n + kTile - 1) / kTile;
+        }
+        hpre[m] = acc;
+        const uint64_t ntiles = acc;
+        const size_t bytes = (size_t)m * sizeof(Desc) + (3 * (size_t)m + 1) * sizeof(uint64_t);
+        if (cudaMemcpyAsync(sl.d_tab, sl.h_tab, bytes, cudaMemcpyHostToDevice, sl.st) != cudaSuccess)
+            return BSG_ERR_CUDA;
+        const Desc* dd = reinterpret_cast<const Desc*>(sl.d_tab);
+        const uint64_t* doff = reinterpret_cast<const uint64_t*>(sl.d_tab + (size_t)m * sizeof(Desc));
+        const uint64_t* dlen = doff + m;
+        const uint64_t* dpre = dlen + m;
+        const unsigned grid = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)sm_count * 4);
+        ingest_kernel<<<grid, kThreads, 0, sl.st>>>(dd, dpre, m, ntiles, pool);
+        if (cudaGetLastError() != cudaSuccess) return BSG_ERR_CUDA;
+        if (cudaMemsetAsync(sl.d_cursor, 0, sizeof(unsigned long long), sl.st) != cudaSuccess)
+            return BSG_ERR_CUDA;
+        if (bsg::launch_batch(pool, doff, dlen, dpre, m, ntiles, sl.d_cursor, mode, batch_grid,
+                              sl.st) != cudaSuccess)
+            return BSG_ERR_CUDA;
+        egress_kernel<<<grid, kThreads, 0, sl.st>>>(dd, dpre, m, ntiles, pool.out);
+        if (cudaGetLastError() != cudaSuccess) return BSG_ERR_CUDA;
+        if (cudaEventRecord(sl.ev, sl.st) != cudaSuccess) return BSG_ERR_CUDA;
+        return BSG_OK;
+    }
+
+    int enqueue_plain(Slot& sl) {
+        const Request* q = sl.reqs[0];
+        const uint64_t o = q->off;
+        const size_t b = q->r.n * 4;
+        float* ps = const_cast<float*>(pool.s) + o;
+        float* pk = const_cast<float*>(pool.k) + o;
+        float* pr = const_cast<float*>(pool.r) + o;
+        float* pv = const_cast<float*>(pool.v) + o;
+        float* pt = const_cast<float*>(pool.t) + o;
+        int32_t* po = const_cast<int32_t*>(pool.ot) + o;
+        if (cudaMemcpyAsync(ps, q->r.sptprice, b, cudaMemcpyHostToDevice, sl.st) ||
+            cudaMemcpyAsync(pk, q->r.strike, b, cudaMemcpyHostToDevice, sl.st) ||
+            cudaMemcpyAsync(pr, q->r.rate, b, cudaMemcpyHostToDevice, sl.st) ||
+            cudaMemcpyAsync(pv, q->r.volatility, b, cudaMemcpyHostToDevice, sl.st) ||
+            cudaMemcpyAsync(pt, q->r.otime, b, cudaMemcpyHostToDevice, sl.st) ||
+            cudaMemcpyAsync(po, q->r.otype, b, cudaMemcpyHostToDevice, sl.st))
+            return BSG_ERR_CUDA;
+        bsg::SoA a{ps, pk, pr, pv, pt, po, pool.out + o};
+        const bsg::MapCfg cfg{1, 256, 0, 0, 0};
+        if (bsg::launch_map(a, (int64_t)q->r.n, mode, cfg, sm_count, sl.st) != cudaSuccess)
+            return BSG_ERR_CUDA;
+        if (cudaMemcpyAsync(q->r.prices, pool.out + o, b, cudaMemcpyDeviceToHost, sl.st) ||
+            cudaEventRecord(sl.ev, sl.st))
+            return BSG_ERR_CUDA;
+        return BSG_OK;
+    }
+
+    void complete(Request* q, int status, double t, bool free_range) {
+        q->status = status;
+        q->t_done = t;
+        q->state = Q_DONE;
+        if (free_range) pool_free(q->off, q->span);
+        if (status == BSG_OK) {
+            st.completed++;
+            st.options_priced += q->r.n;
+        } else if (status == BSG_ERR_CANCELLED) {
+            st.cancelled++;
+        } else {
+            st.failed++;
+        }
+        if (q->auto_release) {
+            if (q->lat_slot) *q->lat_slot = (status == BSG_OK) ? t - q->t_ref : NAN;
+            reqs.erase(q->id);
+            delete q;
+        }
+    }
+
+    // ------------------------------------------------------- dispatcher
+    void dispatcher() {
+        cudaSetDevice(device);
+        std::unique_lock<std::mutex> lk(mu);
+        for (;;) {
+            cv_disp.wait(lk, [&] { return stop || (!paused && !queue.empty() && free_slot() >= 0); });
+            if (stop) break;
+            const int si = free_slot();
+            Slot& sl = slots[si];
+            sl.reqs.clear();
+            uint64_t opts = 0;
+            const int limit = cfg.plain ? 1 : max_req;
+            while (!queue.empty() && (int)sl.reqs.size() < limit) {
+                Request* q = queue.front();
+                if (cfg.max_batch_options && !sl.reqs.empty() &&
+                    opts + q->r.n > cfg.max_batch_options)
+                    break;
+                uint64_t off;
+                if (!pool_alloc(q->span, &off)) break;  // FIFO: wait for memory
+                q->off = off;
+                q->state = Q_ADMITTED;
+                Desc& d = q->desc;
+                d.off = off;
+                d.n = q->r.n;
+                queue.pop_front();
+                sl.reqs.push_back(q);
+                opts += q->r.n;
+            }
+            if (sl.reqs.empty()) {
+                const uint64_t g0 = free_gen;
+                cv_disp.wait(lk, [&] { return stop || free_gen != g0; });
+                continue;
+            }
+            sl.busy = true;
+            st.batches++;
+            st.max_batch_requests_seen = std::max<uint64_t>(st.max_batch_requests_seen, sl.reqs.size());
+            lk.unlock();
+            const int rc = cfg.plain ? enqueue_plain(sl) : enqueue_batched(sl);
+            lk.lock();
+            if (rc != BSG_OK) {
+                cudaGetLastError();
+                // work already enqueued may still run: keep the ranges and
+                // the slot until the stream drains, then fail the requests
+                lk.unlock();
+                const bool drained = cudaStreamSynchronize(sl.st) == cudaSuccess;
+                lk.lock();
+                const double t = now_s();
+                for (Request* q : sl.reqs) complete(q, rc, t, drained);
+                sl.reqs.clear();
+                sl.busy = !drained;
+                free_gen++;
+                cv_done.notify_all();
+                continue;
+            }
+            st.kernel_launches += cfg.plain ? 1 : 3;
+            inflight.push_back(si);
+            cv_comp.notify_one();
+        }
+    }
+
+    // Bounded wait for one batch: cudaEventQuery with short sleeps.
+    int wait_event(cudaEvent_t ev) {
+        const double t_end = now_s() + batch_timeout;
+        int spins = 0;
+        for (;;) {
+            const cudaError_t e = cudaEventQuery(ev);
+            if (e == cudaSuccess) return BSG_OK;
+            if (e != cudaErrorNotReady) {
+                cudaGetLastError();
+                return BSG_ERR_CUDA;
+            }
+            if (now_s() > t_end) return BSG_ERR_TIMEOUT;
+            if (++spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(10));
+        }
+    }
+
+    // -------------------------------------------------------- completer
+    void completer() {
+        cudaSetDevice(device);
+        std::unique_lock<std::mutex> lk(mu);
+        for (;;) {
+            cv_comp.wait(lk, [&] { return stop || !inflight.empty(); });
+            if (inflight.empty()) {
+                if (stop) break;
+                continue;
+            }
+            const int si = inflight.front();
+            lk.unlock();
+            const int rc = wait_event(slots[si].ev);
+            const double t = now_s();
+            lk.lock();
+            inflight.pop_front();
+            Slot& sl = slots[si];
+            // a batch that overran its bound may still be running: its
+            // requests fail but its pool ranges and slot stay held
+            const bool release = rc != BSG_ERR_TIMEOUT;
+            for (Request* q : sl.reqs) complete(q, rc, t, release);
+            sl.reqs.clear();
+            if (release) sl.busy = false;
+            free_gen++;
+            cv_done.notify_all();
+            cv_disp.notify_one();
+        }
+    }
+};
+
+namespace {
+
+void destroy_resources(bsg_server* s) {
+    for (auto& sl : s->slots) {
+        if (sl.st) cudaStreamSynchronize(sl.st);
+        if (sl.ev) cudaEventDestroy(sl.ev);
+        if (sl.h_tab) cudaFreeHost(sl.h_tab);
+        if (sl.d_tab) cudaFree(sl.d_tab);
+        if (sl.d_cursor) cudaFree(sl.d_cursor);
+        if (sl.st) cudaStreamDestroy(sl.st);
+    }
+    s->slots.clear();
+    for (auto& h : s->hosts)
+        if (h.owned) cudaHostUnregister(reinterpret_cast<void*>(h.b));
+    s->hosts.clear();
+    if (s->d_pool) cudaFree(s->d_pool);
+    s->d_pool = nullptr;
+}
+
+int submit_impl(bsg_server* s, const bsg_request* r, uint64_t* id, bool auto_release,
+                double t_ref, double* lat_slot) {
+    if (!s || !r) return BSG_ERR_INVALID_ARG;
+    if (r->n && (!r->sptprice || !r->strike || !r->rate || !r->volatility || !r->otime ||
+                 !r->otype || !r->prices))
+        return BSG_ERR_INVALID_ARG;
+    const uint64_t span = (r->n + kAlign - 1) / kAlign * kAlign;
+    if (span > s->cap) return BSG_ERR_BUDGET;
+    Request* q = new (std::nothrow) Request();
+    if (!q) return BSG_ERR_OUT_OF_MEMORY;
+    q->r = *r;
+    q->span = span;
+    q->t_ref = t_ref;
+    q->auto_release = auto_release;
+    q->lat_slot = lat_slot;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (!s->cfg.plain && r->n) {
+        const size_t b = r->n * 4;
+        const void* arrs[7] = {r->sptprice, r->strike, r->rate, r->volatility,
+                               r->otime, r->otype, r->prices};
+        for (int j = 0; j < 7; ++j) {
+            const HostRange* h = s->host_range(arrs[j], b);
+            if (!h) {
+                delete q;
+                return BSG_ERR_INVALID_ARG;  // not inside registered host memory
+            }
+            const uintptr_t dev = reinterpret_cast<uintptr_t>(arrs[j]) + h->delta;
+            if (j < 5) q->desc.src[j] = reinterpret_cast<const float*>(dev);
+            else if (j == 5) q->desc.ot = reinterpret_cast<const int32_t*>(dev);
+            else q->desc.out = reinterpret_cast<float*>(dev);
+        }
+    }
+    if (s->stop) {
+        delete q;
+        return BSG_ERR_STATE;
+    }
+    q->id = s->next_id++;
+    s->reqs[q->id] = q;
+    s->st.submitted++;
+    if (id) *id = q->id;
+    if (r->n == 0) {
+        s->complete(q, BSG_OK, now_s(), false);
+        s->cv_done.notify_all();
+        return BSG_OK;
+    }
+    q->state = Q_QUEUED;
+    s->queue.push_back(q);
+    s->cv_disp.notify_one();
+    return BSG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bsg_server_create(bsg_server** out, const bsg_server_config* cfg) {
+    if (!out || !cfg) return BSG_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (cfg->max_inflight < 1 || cfg->max_inflight > 16 || cfg->max_batch_requests < 0 ||
+        cfg->max_batch_requests > 65536 || cfg->budget_bytes < 28 * kAlign)
+        return BSG_ERR_INVALID_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || cfg->device < 0 || cfg->device >= ndev) {
+        cudaGetLastError();
+        return BSG_ERR_NO_DEVICE;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, cfg->device) != cudaSuccess ||
+        !(prop.major == 10 && prop.minor == 3))
+        return BSG_ERR_NO_DEVICE;
+    bsg_server* s = new (std::nothrow) bsg_server();
+    if (!s) return BSG_ERR_OUT_OF_MEMORY;
+    s->cfg = *cfg;
+    s->device = cfg->device;
+    s->sm_count = prop.multiProcessorCount;
+    s->max_req = cfg->max_batch_requests ? cfg->max_batch_requests : 4096;
+    s->batch_timeout = cfg->batch_timeout_s > 0 ? cfg->batch_timeout_s : 30.0;
+    switch (cfg->flags & BSG_MODE_MASK) {
+        case BSG_MODE_FAST: s->mode = bsg::MODE_FAST; break;
+        case BSG_MODE_SFU_REF: s->mode = bsg::MODE_SFU_REF; break;
+        case BSG_MODE_LIBM_REF: s->mode = bsg::MODE_LIBM_REF; break;
+        default: delete s; return BSG_ERR_INVALID_ARG;
+    }
+    s->batch_grid = s->sm_count * bsg::batch_blocks_per_sm();
+    int rc = BSG_OK;
+    do {
+        if (cudaSetDevice(s->device) != cudaSuccess) { rc = BSG_ERR_NO_DEVICE; break; }
+        s->cap = cfg->budget_bytes / 28 / kAlign * kAlign;
+        if (cudaMalloc(&s->d_pool, s->cap * 28) != cudaSuccess) { rc = BSG_ERR_OUT_OF_MEMORY; break; }
+        float* f = reinterpret_cast<float*>(s->d_pool);
+        const uint64_t c = s->cap;
+        s->pool = bsg::SoA{f, f + c, f + 2 * c, f + 3 * c, f + 4 * c,
+                           reinterpret_cast<const int32_t*>(f + 5 * c), f + 6 * c};
+        s->free_list[0] = c;
+        const int nslots = cfg->plain ? 1 : cfg->max_inflight;
+        s->slots.resize(nslots);
+        const size_t tb = table_bytes(s->max_req);
+        for (auto& sl : s->slots) {
+            if (cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking) != cudaSuccess ||
+                cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming) != cudaSuccess) {
+                rc = BSG_ERR_CUDA;
+                break;
+            }
+            if (cudaMallocHost(&sl.h_tab, tb) != cudaSuccess || cudaMalloc(&sl.d_tab, tb) != cudaSuccess ||
+                cudaMalloc(&sl.d_cursor, 256) != cudaSuccess) {
+                rc = BSG_ERR_OUT_OF_MEMORY;
+                break;
+            }
+        }
+    } while (0);
+    if (rc != BSG_OK) {
+        cudaGetLastError();
+        destroy_resources(s);
+        delete s;
+        return rc;
+    }
+    s->disp = std::thread([s] { s->dispatcher(); });
+    s->comp = std::thread([s] { s->completer(); });
+    *out = s;
+    return BSG_OK;
+}
+
+void bsg_server_destroy(bsg_server* s) {
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        const double t = now_s();
+        while (!s->queue.empty()) {
+            Request* q = s->queue.front();
+            s->queue.pop_front();
+            s->complete(q, BSG_ERR_CANCELLED, t, false);
+        }
+    }
+    // let in-flight batches complete, then stop the threads
+    {
+        std::unique_lock<std::mutex> lk(s->mu);
+        s->cv_done.wait_for(lk, std::chrono::duration<double>(s->batch_timeout + 1.0),
+                            [&] { return s->inflight.empty(); });
+        s->stop = true;
+    }
+    s->cv_disp.notify_all();
+    s->cv_comp.notify_all();
+    if (s->disp.joinable()) s->disp.join();
+    if (s->comp.joinable()) s->comp.join();
+    cudaSetDevice(s->device);
+    destroy_resources(s);
+    for (auto& kv : s->reqs) delete kv.second;
+    s->reqs.clear();
+    delete s;
+}
+
+int bsg_server_register(bsg_server* s, void* ptr, size_t bytes) {
+    if (!s || !ptr || !bytes) return BSG_ERR_INVALID_ARG;
+    cudaSetDevice(s->device);
+    bool owned = false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) cudaGetLastError();
+    else if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged)
+        return BSG_ERR_INVALID_ARG;
+    if (!(cudaPointerGetAttributes(&a, ptr) == cudaSuccess && a.type == cudaMemoryTypeHost)) {
+        cudaGetLastError();
+        const cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterMapped);
+        if (e == cudaErrorHostMemoryAlreadyRegistered) {
+            cudaGetLastError();
+        } else if (e != cudaSuccess) {
+            cudaGetLastError();
+            return BSG_ERR_CUDA;
+        } else {
+            owned = true;
+        }
+    }
+    if (!owned) {
+        // already pinned by someone else: the whole range must lie inside
+        // that allocation, or the GPU could touch unpinned pages
+        uintptr_t rb = 0;
+        size_t rs = 0;
+        const uintptr_t pb = reinterpret_cast<uintptr_t>(ptr);
+        if (!cuda_range(ptr, &rb, &rs) || pb < rb || pb + bytes > rb + rs) {
+            cudaGetLastError();
+            return BSG_ERR_INVALID_ARG;
+        }
+    }
+    void* dptr = nullptr;
+    if (cudaHostGetDevicePointer(&dptr, ptr, 0) != cudaSuccess || !dptr) {
+        cudaGetLastError();
+        if (owned) cudaHostUnregister(ptr);
+        return BSG_ERR_CUDA;
+    }
+    HostRange h;
+    h.b = reinterpret_cast<uintptr_t>(ptr);
+    h.e = h.b + bytes;
+    h.delta = reinterpret_cast<intptr_t>(dptr) - static_cast<intptr_t>(h.b);
+    h.owned = owned;
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->hosts.push_back(h);
+    return BSG_OK;
+}
+
+int bsg_server_submit(bsg_server* s, const bsg_request* r, uint64_t* id) {
+    return submit_impl(s, r, id, false, now_s(), nullptr);
+}
+
+int bsg_server_wait(bsg_server* s, uint64_t id, double timeout_s, double* latency_s) {
+    if (!s) return BSG_ERR_INVALID_ARG;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return BSG_ERR_INVALID_ARG;
+    Request* q = it->second;
+    auto done = [&] { return q->state == Q_DONE; };
+    if (timeout_s < 0) s->cv_done.wait(lk, done);
+    else if (!s->cv_done.wait_for(lk, std::chrono::duration<double>(timeout_s), done))
+        return BSG_ERR_TIMEOUT;
+    const int status = q->status;
+    if (latency_s) *latency_s = q->t_done - q->t_ref;
+    s->reqs.erase(id);
+    delete q;
+    return status;
+}
+
+int bsg_server_cancel(bsg_server* s, uint64_t id) {
+    if (!s) return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return BSG_ERR_INVALID_ARG;
+    Request* q = it->second;
+    if (q->state != Q_QUEUED) return BSG_ERR_STATE;
+    s->queue.erase(std::find(s->queue.begin(), s->queue.end(), q));
+    s->complete(q, BSG_ERR_CANCELLED, now_s(), false);
+    s->cv_done.notify_all();
+    s->cv_disp.notify_one();
+    return BSG_OK;
+}
+
+int bsg_server_pause(bsg_server* s, int paused) {
+    if (!s) return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->paused = paused != 0;
+    s->cv_disp.notify_one();
+    return BSG_OK;
+}
+
+int bsg_server_get_stats(bsg_server* s, bsg_server_stats* out) {
+    if (!s || !out) return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    *out = s->st;
+    out->queued = s->queue.size();
+    uint64_t in = 0;
+    for (int si : s->inflight) in += s->slots[si].reqs.size();
+    out->inflight_requests = in;
+    return BSG_OK;
+}
+
+int bsg_serve_trace(const bsg_server_config* cfg, const bsg_trace_config* tr,
+                    bsg_trace_result* out, double* lat_out, size_t lat_cap) {
+    if (!cfg || !tr || !out) return BSG_ERR_INVALID_ARG;
+    if (!(tr->rate_per_s > 0) || !(tr->duration_s > 0) || tr->min_n < 1 || tr->max_n < tr->min_n ||
+        tr->max_n > tr->pool_n || !tr->sptprice || !tr->strike || !tr->rate || !tr->volatility ||
+        !tr->otime || !tr->otype || !tr->prices)
+        return BSG_ERR_INVALID_ARG;
+    std::memset(out, 0, sizeof(*out));
+    // the arrival schedule (Poisson), sizes (log-uniform) and pool offsets
+    std::mt19937_64 rng(tr->seed);
+    std::exponential_distribution<double> gap(tr->rate_per_s);
+    std::uniform_real_distribution<double> u(0.0, 1.0);
+    std::vector<double> at;
+    std::vector<uint64_t> ns, offs;
+    const double lmin = std::log((double)tr->min_n), lmax = std::log((double)tr->max_n + 1.0);
+    for (double t = gap(rng); t < tr->duration_s; t += gap(rng)) {
+        uint64_t n = (uint64_t)std::floor(std::exp(lmin + (lmax - lmin) * u(rng)));
+        n = std::min<uint64_t>(std::max<uint64_t>(n, tr->min_n), tr->max_n);
+        const uint64_t room = tr->pool_n - n;
+        const uint64_t o = (uint64_t)(u(rng) * (double)(room + 1)) & ~3ull;
+        at.push_back(t);
+        ns.push_back(n);
+        offs.push_back(std::min(o, room));
+    }
+    const size_t count = at.size();
+    std::vector<double> lat(count, NAN);
+    bsg_server* s = nullptr;
+    int rc = bsg_server_create(&s, cfg);
+    if (rc) return rc;
+    const size_t pb = tr->pool_n * 4;
+    const void* arrs[7] = {tr->sptprice, tr->strike, tr->rate, tr->volatility, tr->otime,
+                           tr->otype, tr->prices};
+    for (int j = 0; j < 7 && rc == BSG_OK; ++j) rc = bsg_server_register(s, const_cast<void*>(arrs[j]), pb);
+    if (rc) {
+        bsg_server_destroy(s);
+        return rc;
+    }
+    const double t0 = now_s() + 0.02;
+    double late = 0.0;
+    uint64_t submitted = 0;
+    for (size_t k = 0; k < count; ++k) {
+        const double ts = t0 + at[k];
+        double tn = now_s();
+        if (tn < ts) {
+            if (ts - tn > 200e-6)
+                std::this_thread::sleep_for(std::chrono::duration<double>(ts - tn - 100e-6));
+            while (now_s() < ts) {
+            }
+        } else {
+            late = std::max(late, tn - ts);
+        }
+        const uint64_t o = offs[k];
+        bsg_request r{tr->sptprice + o, tr->strike + o, tr->rate + o, tr->volatility + o,
+                      tr->otime + o, tr->otype + o, tr->prices + o, ns[k]};
+        if (submit_impl(s, &r, nullptr, true, ts, &lat[k]) == BSG_OK) submitted++;
+    }
+    // drain (bounded)
+    const double drain = tr->drain_timeout_s > 0 ? tr->drain_timeout_s : 60.0;
+    {
+        std::unique_lock<std::mutex> lk(s->mu);
+        s->cv_done.wait_for(lk, std::chrono::duration<double>(drain), [&] {
+            return s->st.completed + s->st.failed + s->st.cancelled >= submitted;
+        });
+    }
+    bsg_server_stats stt;
+    bsg_server_get_stats(s, &stt);
+    bsg_server_destroy(s);  // cancels anything left
+    // statistics over completed requests
+    std::vector<double> ok;
+    ok.reserve(count);
+    uint64_t opts = 0;
+    double t_last = t0;
+    for (size_t k = 0; k < count; ++k) {
+        if (std::isnan(lat[k])) continue;
+        ok.push_back(lat[k]);
+        opts += ns[k];
+        t_last = std::max(t_last, t0 + at[k] + lat[k]);
+    }
+    std::sort(ok.begin(), ok.end());
+    auto pct = [&](double p) -> double {
+        if (ok.empty()) return (double)NAN;
+        size_t i = (size_t)std::ceil(p * (double)ok.size()) - 1;
+        return ok[std::min(i, ok.size() - 1)];
+    };
+    out->requests = count;
+    out->completed = ok.size();
+    out->failed = count - ok.size();
+    out->options = opts;
+    out->wall_s = t_last - t0;
+    out->options_per_s = out->wall_s > 0 ? (double)opts / out->wall_s : 0.0;
+    out->requests_per_s = out->wall_s > 0 ? (double)ok.size() / out->wall_s : 0.0;
+    out->p50_s = pct(0.50);
+    out->p99_s = pct(0.99);
+    out->p999_s = pct(0.999);
+    out->max_s = ok.empty() ? NAN : ok.back();
+    double sum = 0;
+    for (double x : ok) sum += x;
+    out->mean_s = ok.empty() ? NAN : sum / (double)ok.size();
+    out->batches = stt.batches;
+    out->mean_batch_requests = stt.batches ? (double)stt.completed / (double)stt.batches : 0.0;
+    out->late_submit_max_s = late;
+    if (lat_out)
+        for (size_t k = 0; k < std::min(lat_cap, count); ++k) lat_out[k] = lat[k];
+    return BSG_OK;
+}
+
+}  // extern "C"
