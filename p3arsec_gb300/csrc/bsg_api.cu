@@ -81,7 +81,8 @@ struct bsg_ctx {
     size_t seg_cap = 0;
     uint64_t* h_seg = nullptr;  // pinned staging of the same layout
     cudaEvent_t seg_ev = nullptr;
-    unsigned long long* d_cursor = nullptr;
+    unsigned long long* d_cursor = nullptr;  // one work counter per pass
+    size_t cursor_cap = 0;
     // error-report scratch
     bsg::ErrAcc* d_acc = nullptr;
     double* d_edges = nullptr;
@@ -383,7 +384,8 @@ int bsg_create(bsg_ctx** out, int device, size_t max_options) {
         c->cap = max_options;
         c->cap_al = round_up(std::max<size_t>(max_options, 1), 64);  // 256-byte aligned arrays
         if (cudaMalloc(&c->dev_buf, 7 * c->cap_al * sizeof(float)) != cudaSuccess) { rc = BSG_ERR_OUT_OF_MEMORY; break; }
-        if (cudaMalloc(&c->d_cursor, 256) != cudaSuccess) { rc = BSG_ERR_OUT_OF_MEMORY; break; }
+        c->cursor_cap = 128;
+        if (cudaMalloc(&c->d_cursor, c->cursor_cap * 8) != cudaSuccess) { rc = BSG_ERR_OUT_OF_MEMORY; break; }
         if (cudaMalloc(&c->d_acc, sizeof(bsg::ErrAcc) * bsg::kMaxErrBuckets) != cudaSuccess) { rc = BSG_ERR_OUT_OF_MEMORY; break; }
         if (cudaMalloc(&c->d_edges, sizeof(double) * (bsg::kMaxErrBuckets + 1)) != cudaSuccess) { rc = BSG_ERR_OUT_OF_MEMORY; break; }
         const int bps = bsg::batch_blocks_per_sm();
@@ -562,17 +564,29 @@ int bsg_price_batch(bsg_ctx* c, const float* s, const float* k, const float* r,
         BSG_CK(c, cudaMemcpyAsync((void*)d_pre, c->h_seg + 2 * c->seg_cap, (m + 1) * 8, cudaMemcpyHostToDevice, c->stream));
         BSG_CK(c, cudaEventRecord(c->seg_ev, c->stream));
         const int grid = c->sm_count * c->batch_blocks_per_sm;
-        auto one_run = [&]() -> cudaError_t {
-            cudaError_t e = cudaMemsetAsync(c->d_cursor, 0, sizeof(unsigned long long), c->stream);
-            if (e != cudaSuccess) return e;
-            return bsg::launch_batch(a, d_off, d_len, d_pre, m, ntiles, c->d_cursor, mode, grid, c->stream);
+        const uint64_t topt = bsg::batch_tile_options();
+        // one work counter per pass, zeroed together, so that pass j + 1 can
+        // start (PDL) while pass j drains
+        if ((size_t)num_runs > c->cursor_cap) {
+            BSG_CK(c, cudaStreamSynchronize(c->stream));
+            graph_drop_all(c);
+            cudaFree(c->d_cursor);
+            c->d_cursor = nullptr;
+            c->cursor_cap = 0;
+            BSG_CK(c, cudaMalloc(&c->d_cursor, (size_t)num_runs * 8));
+            c->cursor_cap = (size_t)num_runs;
+        }
+        auto all_runs = [&]() -> cudaError_t {
+            cudaError_t e = cudaMemsetAsync(c->d_cursor, 0, (size_t)num_runs * 8, c->stream);
+            for (int j = 0; j < num_runs && e == cudaSuccess; ++j)
+                e = bsg::launch_batch(a, d_off, d_len, d_pre, m, ntiles, topt, c->d_cursor + j,
+                                      mode, grid, j > 0 ? 1 : 0, c->stream);
+            return e;
         };
         if (num_runs == 1 || (flags & BSG_NO_GRAPH)) {
-            for (int j = 0; j < num_runs; ++j) {
-                cudaError_t e = one_run();
-                if (e != cudaSuccess) return cuda_fail(c, e, "launch_batch");
-                c->launches++;
-            }
+            cudaError_t e = all_runs();
+            if (e != cudaSuccess) return cuda_fail(c, e, "launch_batch");
+            c->launches += (uint64_t)num_runs;
             return finish(c, flags);
         }
         GraphKey key = make_key(a, (int64_t)pool_len, num_runs, mode, c->tune, 1, ntiles, m);
@@ -580,8 +594,7 @@ int bsg_price_batch(bsg_ctx* c, const float* s, const float* k, const float* r,
         if (!exec) {
             cudaGraph_t g = nullptr;
             BSG_CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-            cudaError_t le = cudaSuccess;
-            for (int j = 0; j < num_runs && le == cudaSuccess; ++j) le = one_run();
+            cudaError_t le = all_runs();
             cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
             if (le != cudaSuccess) {
                 if (g) cudaGraphDestroy(g);

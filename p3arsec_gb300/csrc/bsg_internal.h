@@ -53,13 +53,16 @@ cudaError_t launch_fp64(const SoA& a, double* out, int64_t n, int sm_count,
                         cudaStream_t st);
 
 // Persistent batched pricing.  seg_off/seg_len/tile_prefix are device arrays
-// of nseg (tile_prefix: nseg + 1 entries, exclusive prefix of tiles per
-// segment); cursor is a device counter that must be 0 at launch.
+// of nseg (tile_prefix: nseg + 1 entries, exclusive prefix of tiles of
+// tile_opts options per segment); cursor is a device counter that must be 0
+// at launch.  pdl: launch with programmatic stream serialization (the next
+// pass may start while this one drains; it must use its own cursor).
 cudaError_t launch_batch(const SoA& pool, const uint64_t* seg_off,
                          const uint64_t* seg_len, const uint64_t* tile_prefix,
-                         int nseg, uint64_t ntiles, unsigned long long* cursor,
-                         int mode, int grid, cudaStream_t st);
-// Options per batch tile (fixed by the batch kernel's shape).
+                         int nseg, uint64_t ntiles, uint64_t tile_opts,
+                         unsigned long long* cursor, int mode, int grid, int pdl,
+                         cudaStream_t st);
+// Default options per batch tile.
 uint64_t batch_tile_options();
 // Resident blocks per SM of the batch kernel (its persistent grid = this x SMs).
 int batch_blocks_per_sm();

@@ -281,11 +281,11 @@ __device__ __forceinline__ void price_range(const SoA& pool, uint64_t b, uint64_
 template <int M>
 __global__ void __launch_bounds__(kBatchBlock) batch_kernel(
     SoA pool, const uint64_t* __restrict__ seg_off, const uint64_t* __restrict__ seg_len,
-    const uint64_t* __restrict__ tile_prefix, int nseg, uint64_t ntiles,
+    const uint64_t* __restrict__ tile_prefix, int nseg, uint64_t ntiles, uint64_t topt,
     unsigned long long* cursor) {
     __shared__ uint64_t sh_b, sh_e;
     __shared__ int sh_done;
-    const uint64_t topt = kBatchTileOptions;
+    pdl_trigger();
     for (;;) {
         if (threadIdx.x == 0) {
             const unsigned long long tile = atomicAdd(cursor, 1ull);
@@ -311,6 +311,7 @@ __global__ void __launch_bounds__(kBatchBlock) batch_kernel(
         if (done) break;
         price_range<M>(pool, b, e);
     }
+    pdl_wait();
 }
 
 int batch_blocks_per_sm() {
@@ -324,23 +325,34 @@ int batch_blocks_per_sm() {
 
 cudaError_t launch_batch(const SoA& pool, const uint64_t* seg_off,
                          const uint64_t* seg_len, const uint64_t* tile_prefix,
-                         int nseg, uint64_t ntiles, unsigned long long* cursor,
-                         int mode, int grid, cudaStream_t st) {
+                         int nseg, uint64_t ntiles, uint64_t tile_opts,
+                         unsigned long long* cursor, int mode, int grid, int pdl,
+                         cudaStream_t st) {
     if (ntiles == 0 || nseg <= 0) return cudaSuccess;
+    if (tile_opts == 0) return cudaErrorInvalidValue;
+    if ((uint64_t)grid > ntiles) grid = (int)ntiles;  // no block without a tile
     if (grid < 1) grid = 1;
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned)grid);
+    lc.blockDim = dim3(kBatchBlock);
+    lc.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    lc.attrs = attr;
+    lc.numAttrs = pdl ? 1 : 0;
     switch (mode) {
         case MODE_FAST:
-            batch_kernel<MODE_FAST><<<grid, kBatchBlock, 0, st>>>(pool, seg_off, seg_len, tile_prefix, nseg, ntiles, cursor);
-            break;
+            return cudaLaunchKernelEx(&lc, batch_kernel<MODE_FAST>, pool, seg_off, seg_len,
+                                      tile_prefix, nseg, ntiles, tile_opts, cursor);
         case MODE_SFU_REF:
-            batch_kernel<MODE_SFU_REF><<<grid, kBatchBlock, 0, st>>>(pool, seg_off, seg_len, tile_prefix, nseg, ntiles, cursor);
-            break;
+            return cudaLaunchKernelEx(&lc, batch_kernel<MODE_SFU_REF>, pool, seg_off, seg_len,
+                                      tile_prefix, nseg, ntiles, tile_opts, cursor);
         case MODE_LIBM_REF:
-            batch_kernel<MODE_LIBM_REF><<<grid, kBatchBlock, 0, st>>>(pool, seg_off, seg_len, tile_prefix, nseg, ntiles, cursor);
-            break;
+            return cudaLaunchKernelEx(&lc, batch_kernel<MODE_LIBM_REF>, pool, seg_off, seg_len,
+                                      tile_prefix, nseg, ntiles, tile_opts, cursor);
         default: return cudaErrorInvalidValue;
     }
-    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------- error report

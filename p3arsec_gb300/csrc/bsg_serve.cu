@@ -39,7 +39,8 @@
 
 namespace {
 
-constexpr uint64_t kTile = 8192;   // options per ingest/egress/batch tile
+constexpr uint64_t kTile = 2048;   // options per ingest/egress/batch tile: small,
+                                   // so one request spreads over many SMs
 constexpr uint64_t kAlign = 64;    // pool ranges start 256-byte aligned
 constexpr int kThreads = 256;
 
@@ -56,6 +57,7 @@ struct Desc {
     float* out;
     uint64_t off;  // pool offset in options
     uint64_t n;
+    uint64_t vec;  // 1: every host array 16-byte aligned (float4 transfers)
 };
 
 __device__ __forceinline__ int find_segment(const uint64_t* pre, int m, uint64_t tile) {
@@ -84,7 +86,19 @@ __global__ void __launch_bounds__(kThreads) ingest_kernel(const Desc* __restrict
         const Desc q = d[sh_q];
         const uint64_t b = (tile - pre[sh_q]) * kTile;
         const uint64_t e = (b + kTile < q.n) ? b + kTile : q.n;
-        for (uint64_t i = b + threadIdx.x; i < e; i += kThreads) {
+        // float4 body when the host arrays allow it (pool offsets are 64-
+        // option aligned and b is a multiple of 4), scalar rest
+        const uint64_t e4 = q.vec ? b + ((e - b) & ~3ull) : b;
+        for (uint64_t g = b / 4 + threadIdx.x; g < e4 / 4; g += kThreads) {
+            const uint64_t o = q.off / 4 + g;
+            reinterpret_cast<float4*>(ps)[o] = reinterpret_cast<const float4*>(q.src[0])[g];
+            reinterpret_cast<float4*>(pk)[o] = reinterpret_cast<const float4*>(q.src[1])[g];
+            reinterpret_cast<float4*>(pr)[o] = reinterpret_cast<const float4*>(q.src[2])[g];
+            reinterpret_cast<float4*>(pv)[o] = reinterpret_cast<const float4*>(q.src[3])[g];
+            reinterpret_cast<float4*>(pt)[o] = reinterpret_cast<const float4*>(q.src[4])[g];
+            reinterpret_cast<int4*>(po)[o] = reinterpret_cast<const int4*>(q.ot)[g];
+        }
+        for (uint64_t i = e4 + threadIdx.x; i < e; i += kThreads) {
             const uint64_t o = q.off + i;
             ps[o] = q.src[0][i];
             pk[o] = q.src[1][i];
@@ -109,7 +123,10 @@ __global__ void __launch_bounds__(kThreads) egress_kernel(const Desc* __restrict
         const Desc q = d[sh_q];
         const uint64_t b = (tile - pre[sh_q]) * kTile;
         const uint64_t e = (b + kTile < q.n) ? b + kTile : q.n;
-        for (uint64_t i = b + threadIdx.x; i < e; i += kThreads) q.out[i] = pool_out[q.off + i];
+        const uint64_t e4 = q.vec ? b + ((e - b) & ~3ull) : b;
+        for (uint64_t g = b / 4 + threadIdx.x; g < e4 / 4; g += kThreads)
+            reinterpret_cast<float4*>(q.out)[g] = reinterpret_cast<const float4*>(pool_out)[q.off / 4 + g];
+        for (uint64_t i = e4 + threadIdx.x; i < e; i += kThreads) q.out[i] = pool_out[q.off + i];
         __syncthreads();
     }
 }
@@ -267,13 +284,13 @@ struct bsg_server {
         const uint64_t* doff = reinterpret_cast<const uint64_t*>(sl.d_tab + (size_t)m * sizeof(Desc));
         const uint64_t* dlen = doff + m;
         const uint64_t* dpre = dlen + m;
-        const unsigned grid = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)sm_count * 4);
+        const unsigned grid = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)sm_count * 8);
         ingest_kernel<<<grid, kThreads, 0, sl.st>>>(dd, dpre, m, ntiles, pool);
         if (cudaGetLastError() != cudaSuccess) return BSG_ERR_CUDA;
         if (cudaMemsetAsync(sl.d_cursor, 0, sizeof(unsigned long long), sl.st) != cudaSuccess)
             return BSG_ERR_CUDA;
-        if (bsg::launch_batch(pool, doff, dlen, dpre, m, ntiles, sl.d_cursor, mode, batch_grid,
-                              sl.st) != cudaSuccess)
+        if (bsg::launch_batch(pool, doff, dlen, dpre, m, ntiles, kTile, sl.d_cursor, mode,
+                              batch_grid, 0, sl.st) != cudaSuccess)
             return BSG_ERR_CUDA;
         egress_kernel<<<grid, kThreads, 0, sl.st>>>(dd, dpre, m, ntiles, pool.out);
         if (cudaGetLastError() != cudaSuccess) return BSG_ERR_CUDA;
@@ -470,6 +487,7 @@ int submit_impl(bsg_server* s, const bsg_request* r, uint64_t* id, bool auto_rel
     q->lat_slot = lat_slot;
     std::lock_guard<std::mutex> lk(s->mu);
     if (!s->cfg.plain && r->n) {
+        bool vec = true;
         const size_t b = r->n * 4;
         const void* arrs[7] = {r->sptprice, r->strike, r->rate, r->volatility,
                                r->otime, r->otype, r->prices};
@@ -480,10 +498,12 @@ int submit_impl(bsg_server* s, const bsg_request* r, uint64_t* id, bool auto_rel
                 return BSG_ERR_INVALID_ARG;  // not inside registered host memory
             }
             const uintptr_t dev = reinterpret_cast<uintptr_t>(arrs[j]) + h->delta;
+            if ((dev & 15) != 0) vec = false;
             if (j < 5) q->desc.src[j] = reinterpret_cast<const float*>(dev);
             else if (j == 5) q->desc.ot = reinterpret_cast<const int32_t*>(dev);
             else q->desc.out = reinterpret_cast<float*>(dev);
         }
+        q->desc.vec = vec ? 1 : 0;
     }
     if (s->stop) {
         delete q;
