@@ -262,14 +262,20 @@ constexpr uint64_t kBatchTileOptions = 8192;
 uint64_t batch_tile_options() { return kBatchTileOptions; }
 
 // Prices options [b, e) of the pool with the whole block: an unaligned head
-// and tail one option per thread, the 16-byte aligned body in v4 groups.
-template <int M>
+// and tail one option per thread, the aligned body in groups of W options
+// (W = 4: 16-byte loads, VPT = 2 groups per thread; W = 8: 256-bit loads,
+// one group per thread).
+template <int M, int W>
 __device__ __forceinline__ void price_range(const SoA& pool, uint64_t b, uint64_t e) {
-    const uint64_t head_end = ((b + 3) & ~3ull) < e ? ((b + 3) & ~3ull) : e;
-    const uint64_t body_end = (e & ~3ull) > head_end ? (e & ~3ull) : head_end;
+    constexpr uint64_t mask = W - 1;
+    const uint64_t head_end = ((b + mask) & ~mask) < e ? ((b + mask) & ~mask) : e;
+    const uint64_t body_end = (e & ~mask) > head_end ? (e & ~mask) : head_end;
     const uint64_t i_head = b + threadIdx.x;
     if (i_head < head_end) price_scalar<M>(pool, (int64_t)i_head);
-    price_groups<M, 4, kBatchVpt, 0>(pool, (int64_t)(head_end / 4), (int64_t)(body_end / 4), 0ull);
+    if constexpr (W == 8)
+        price_groups<M, 8, 1, 2>(pool, (int64_t)(head_end / 8), (int64_t)(body_end / 8), 0ull);
+    else
+        price_groups<M, 4, kBatchVpt, 0>(pool, (int64_t)(head_end / 4), (int64_t)(body_end / 4), 0ull);
     const uint64_t i_tail = body_end + threadIdx.x;
     if (i_tail < e) price_scalar<M>(pool, (int64_t)i_tail);
 }
@@ -278,7 +284,7 @@ __device__ __forceinline__ void price_range(const SoA& pool, uint64_t b, uint64_
 // counter, maps it to its segment by binary search over the tile prefix and
 // prices it.  No block ever waits on another; the loop ends when the counter
 // passes the last tile.
-template <int M>
+template <int M, int W>
 __global__ void __launch_bounds__(kBatchBlock) batch_kernel(
     SoA pool, const uint64_t* __restrict__ seg_off, const uint64_t* __restrict__ seg_len,
     const uint64_t* __restrict__ tile_prefix, int nseg, uint64_t ntiles, uint64_t topt,
@@ -309,14 +315,14 @@ __global__ void __launch_bounds__(kBatchBlock) batch_kernel(
         const uint64_t b = sh_b, e = sh_e;
         __syncthreads();
         if (done) break;
-        price_range<M>(pool, b, e);
+        price_range<M, W>(pool, b, e);
     }
     pdl_wait();
 }
 
 int batch_blocks_per_sm() {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<MODE_FAST>, kBatchBlock, 0) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel<MODE_FAST, 8>, kBatchBlock, 0) != cudaSuccess) {
         cudaGetLastError();
         return 1;
     }
@@ -341,18 +347,20 @@ cudaError_t launch_batch(const SoA& pool, const uint64_t* seg_off,
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     lc.attrs = attr;
     lc.numAttrs = pdl ? 1 : 0;
+    // 256-bit loads need every pool array 32-byte aligned
+    const bool w8 = map_vectorizable(pool, MapCfg{1, kBatchBlock, 0, 2, 0});
+#define BSG_BATCH(M_) \
+    (w8 ? cudaLaunchKernelEx(&lc, batch_kernel<M_, 8>, pool, seg_off, seg_len, tile_prefix, nseg, \
+                             ntiles, tile_opts, cursor) \
+        : cudaLaunchKernelEx(&lc, batch_kernel<M_, 4>, pool, seg_off, seg_len, tile_prefix, nseg, \
+                             ntiles, tile_opts, cursor))
     switch (mode) {
-        case MODE_FAST:
-            return cudaLaunchKernelEx(&lc, batch_kernel<MODE_FAST>, pool, seg_off, seg_len,
-                                      tile_prefix, nseg, ntiles, tile_opts, cursor);
-        case MODE_SFU_REF:
-            return cudaLaunchKernelEx(&lc, batch_kernel<MODE_SFU_REF>, pool, seg_off, seg_len,
-                                      tile_prefix, nseg, ntiles, tile_opts, cursor);
-        case MODE_LIBM_REF:
-            return cudaLaunchKernelEx(&lc, batch_kernel<MODE_LIBM_REF>, pool, seg_off, seg_len,
-                                      tile_prefix, nseg, ntiles, tile_opts, cursor);
+        case MODE_FAST: return BSG_BATCH(MODE_FAST);
+        case MODE_SFU_REF: return BSG_BATCH(MODE_SFU_REF);
+        case MODE_LIBM_REF: return BSG_BATCH(MODE_LIBM_REF);
         default: return cudaErrorInvalidValue;
     }
+#undef BSG_BATCH
 }
 
 // ---------------------------------------------------------- error report
