@@ -501,6 +501,73 @@ def run_serve(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- file I/O
+def run_io(args, rank, world, local):
+    """The reference's file formats: parallel parse / write of libbsgpu.so vs
+    the reference's sequential fscanf / fprintf loops (oracle restatement),
+    same files, results checked byte for byte."""
+    import shutil
+
+    import oracle
+    from p3arsec_gb300 import abi, books
+    from p3arsec_gb300 import build as b
+    b.build()
+    oracle.build(ref=False)
+    if rank != 0:
+        return
+    n = args.n
+    book = books.generate(n, seed=SEED + 7)
+    prices = oracle.price_ref(book.slice(0, min(n, 1 << 20)))
+    prices = np.resize(prices, n).astype(np.float32)
+    d = tempfile.mkdtemp(prefix="bsg_io_")
+    try:
+        inp = os.path.join(d, "in.txt")
+        t0 = time.perf_counter()
+        abi.write_parsec_input(inp, book)
+        t_gen = time.perf_counter() - t0
+        mb_in = os.path.getsize(inp) / 1e6
+        threads = os.cpu_count() or 1
+        best = 1e30
+        for _ in range(3):
+            t0 = time.perf_counter()
+            got, _ = abi.read_parsec(inp)
+            best = min(best, time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        ref, _ = oracle.read_parsec_fscanf(inp, n)
+        t_ref = time.perf_counter() - t0
+        same_in = all(np.array_equal(x.view(np.uint32), y.view(np.uint32))
+                      for x, y in zip(got.arrays(), ref.arrays()))
+        o1, o2 = os.path.join(d, "o1.txt"), os.path.join(d, "o2.txt")
+        bw = 1e30
+        for _ in range(3):
+            t0 = time.perf_counter()
+            abi.write_parsec_prices(o1, prices)
+            bw = min(bw, time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        oracle.write_prices_fprintf(o2, prices)
+        t_refw = time.perf_counter() - t0
+        mb_out = os.path.getsize(o1) / 1e6
+        with open(o1, "rb") as f1, open(o2, "rb") as f2:
+            same_out = f1.read() == f2.read()
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    line = {
+        "metric": "PARSEC file I/O: options/s parsed and written (reference formats)",
+        "value": n / best, "unit": UNIT, "n_gpus": 0, "higher_is_better": True,
+        "dtype": "f32", "data": "synthetic (seeded book)",
+        "config": {"workload": f"{n} options: parse a {mb_in:.0f} MB input file, write a "
+                               f"{mb_out:.0f} MB %.18f output file", "threads": threads},
+        "parse": {"ours_s": best, "ours_MBps": mb_in / best, "reference_fscanf_s": t_ref,
+                  "speedup": t_ref / best, "bit_identical": same_in},
+        "write": {"ours_s": bw, "ours_MBps": mb_out / bw, "reference_fprintf_s": t_refw,
+                  "speedup": t_refw / bw, "byte_identical": same_out},
+        "input_generation_s": t_gen,
+        "cpu_baseline": {"value": n / t_ref, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": "the reference's fscanf loop (blackscholes.c:726-734) on the same file"},
+    }
+    print(json.dumps(line), flush=True)
+
+
 # ---------------------------------------------------------- reference arm
 def run_reference(args, rank, world, local):
     """The reference's CPU path (the oracle port of its FastFlow map: same
@@ -545,7 +612,7 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=["map", "batch", "precision", "serve"], default="map")
+    ap.add_argument("--config", choices=["map", "batch", "precision", "serve", "io"], default="map")
     ap.add_argument("--serve-rate", type=float, default=20000.0)
     ap.add_argument("--serve-rates",
                     default="1000,5000,10000,15000,20000,30000,40000,50000,60000,70000,80000")
@@ -570,6 +637,8 @@ def main(argv=None):
         run_precision(args, rank, world, local)
     elif args.config == "serve":
         run_serve(args, rank, world, local)
+    elif args.config == "io":
+        run_io(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 

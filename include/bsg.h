@@ -283,6 +283,40 @@ typedef struct bsg_trace_result {
 int bsg_serve_trace(const bsg_server_config* cfg, const bsg_trace_config* trace,
                     bsg_trace_result* out, double* latencies_out, size_t latencies_cap);
 
+/* ---- the reference's file formats (host code) --------------------------
+ * Input, blackscholes.c:695-739: a count ("%i"), then per option
+ * "%f %f %f %f %f %f %c %f %f" = s strike r divq v t OptionType divs
+ * DGrefval; otype = 1 for 'P', else 0 (:760).  Floats convert as the
+ * reference's fscanf does (strtof), so arrays are bit-identical; parsing runs
+ * on nthreads threads (0 = all cores).  Output, :923-947: "%i\n" then
+ * "%.18f\n" per price, byte-identical to the reference's fprintf.  A bsg_book
+ * owns one 256-byte-aligned host allocation (release with bsg_book_free). */
+typedef struct bsg_book {
+    size_t n;
+    float* sptprice;
+    float* strike;
+    float* rate;
+    float* volatility;
+    float* otime;
+    int32_t* otype;
+    float* dgrefval;
+    void* mem_; /* owned allocation */
+} bsg_book;
+
+int bsg_read_parsec(const char* path, int nthreads, bsg_book* out);
+int bsg_parse_parsec(const char* text, size_t len, int nthreads, bsg_book* out);
+void bsg_book_free(bsg_book* book);
+int bsg_write_parsec_prices(const char* path, const float* prices, size_t n, int nthreads);
+/* The output text in memory (release with bsg_text_free). */
+int bsg_format_prices(const float* prices, size_t n, int nthreads, char** text, size_t* len);
+void bsg_text_free(char* text);
+/* An input file in the same format (floats as "%.9g", which round-trips
+ * through "%f"; divq = divs = 0; DGrefval from the book, 0 if NULL). */
+int bsg_write_parsec_input(const char* path, const bsg_book* book, int nthreads);
+/* Binary SoA file ("BSGSOA01", uint64 n, the seven arrays). */
+int bsg_write_soa(const char* path, const bsg_book* book);
+int bsg_read_soa(const char* path, bsg_book* out);
+
 /* ---- tuning ------------------------------------------------------------
  * The plain map is a family of kernels: vector width per thread, block size
  * and grid size.  bsg_autotune times the candidates on the context's device

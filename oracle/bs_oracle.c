@@ -12,6 +12,7 @@
 #include <math.h>
 #include <stdint.h>
 #include <pthread.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <time.h>
 
@@ -261,4 +262,50 @@ double bso_bs_map(int nthreads, int num_runs, size_t n, const float* s,
     pthread_mutex_destroy(&g.mu);
     free(b); free(e); free(ws); free(th);
     return secs;
+}
+
+/* ---- the reference's file I/O, sequential (the I/O baseline) ------------- */
+
+/* blackscholes.c:695-767: fscanf the count and 9 fields per option, then the
+ * SoA build.  Arrays must hold n entries; returns n, or -1 on a read error. */
+long bso_read_parsec_fscanf(const char* path, size_t cap, float* s, float* k,
+                            float* r, float* v, float* t, int32_t* otype,
+                            float* dgrefval)
+{
+    FILE* f = fopen(path, "r");
+    if (!f) return -1;
+    int n = 0;
+    if (fscanf(f, "%i", &n) != 1 || n < 0 || (size_t)n > cap) {
+        fclose(f);
+        return -1;
+    }
+    for (int i = 0; i < n; ++i) {
+        float divq, divs;
+        char type;
+        if (fscanf(f, "%f %f %f %f %f %f %c %f %f", &s[i], &k[i], &r[i], &divq,
+                   &v[i], &t[i], &type, &divs, &dgrefval[i]) != 9) {
+            fclose(f);
+            return -1;
+        }
+        otype[i] = (type == 'P') ? 1 : 0;
+    }
+    fclose(f);
+    return n;
+}
+
+/* blackscholes.c:923-947 */
+int bso_write_prices_fprintf(const char* path, const float* prices, size_t n)
+{
+    FILE* f = fopen(path, "w");
+    if (!f) return -1;
+    if (fprintf(f, "%i\n", (int)n) < 0) {
+        fclose(f);
+        return -1;
+    }
+    for (size_t i = 0; i < n; ++i)
+        if (fprintf(f, "%.18f\n", prices[i]) < 0) {
+            fclose(f);
+            return -1;
+        }
+    return fclose(f) == 0 ? 0 : -1;
 }

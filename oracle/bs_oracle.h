@@ -61,6 +61,13 @@ double bso_bs_map(int nthreads, int num_runs, size_t n, const float* s,
                   const float* k, const float* r, const float* v,
                   const float* t, const int32_t* otype, float* prices);
 
+/* The reference's sequential text I/O (blackscholes.c:695-767, 923-947):
+ * the baseline the parallel I/O of libbsgpu.so is measured against. */
+long bso_read_parsec_fscanf(const char* path, size_t cap, float* s, float* k,
+                            float* r, float* v, float* t, int32_t* otype,
+                            float* dgrefval);
+int bso_write_prices_fprintf(const char* path, const float* prices, size_t n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -59,6 +59,10 @@ def lib() -> ctypes.CDLL:
         L.bso_price_fp64_soa.argtypes = [ctypes.c_size_t] + [_P] * 7
         L.bso_static_partition.restype = None
         L.bso_static_partition.argtypes = [ctypes.c_int64, ctypes.c_int, _P, _P]
+        L.bso_read_parsec_fscanf.restype = ctypes.c_long
+        L.bso_read_parsec_fscanf.argtypes = [ctypes.c_char_p, ctypes.c_size_t] + [_P] * 7
+        L.bso_write_prices_fprintf.restype = ctypes.c_int
+        L.bso_write_prices_fprintf.argtypes = [ctypes.c_char_p, _P, ctypes.c_size_t]
         L.bso_bs_map.restype = ctypes.c_double
         L.bso_bs_map.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_size_t] + [_P] * 7
         _lib = L
@@ -130,6 +134,24 @@ def static_partition(n: int, nw: int):
     e = np.empty(nw, dtype=np.int64)
     lib().bso_static_partition(n, nw, _p(b), _p(e))
     return b, e
+
+
+def read_parsec_fscanf(path, cap: int):
+    """The reference's sequential parse; returns (Book, dgrefval)."""
+    from p3arsec_gb300.books import Book
+    a = [np.empty(cap, np.float32) for _ in range(5)]
+    ot = np.empty(cap, np.int32)
+    dg = np.empty(cap, np.float32)
+    n = lib().bso_read_parsec_fscanf(os.fsencode(str(path)), cap, *[_p(x) for x in a], _p(ot), _p(dg))
+    if n < 0:
+        raise RuntimeError(f"cannot read {path}")
+    return Book(*(x[:n] for x in a), ot[:n]), dg[:n]
+
+
+def write_prices_fprintf(path, prices):
+    p = np.ascontiguousarray(prices, dtype=np.float32)
+    if lib().bso_write_prices_fprintf(os.fsencode(str(path)), _p(p), len(p)) != 0:
+        raise RuntimeError(f"cannot write {path}")
 
 
 def bs_map(book, nthreads: int, num_runs: int):

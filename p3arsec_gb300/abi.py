@@ -109,6 +109,14 @@ class TraceResult(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class BookC(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_size_t), ("sptprice", ctypes.c_void_p),
+                ("strike", ctypes.c_void_p), ("rate", ctypes.c_void_p),
+                ("volatility", ctypes.c_void_p), ("otime", ctypes.c_void_p),
+                ("otype", ctypes.c_void_p), ("dgrefval", ctypes.c_void_p),
+                ("mem_", ctypes.c_void_p)]
+
+
 # Every symbol the header declares, with its ctypes signature.
 _P = ctypes.c_void_p
 _SZ = ctypes.c_size_t
@@ -140,6 +148,16 @@ SIGNATURES = {
     "bsg_server_get_stats": (_I, [_P, ctypes.POINTER(ServerStats)]),
     "bsg_serve_trace": (_I, [ctypes.POINTER(ServerConfig), ctypes.POINTER(TraceConfig),
                              ctypes.POINTER(TraceResult), _P, _SZ]),
+    "bsg_read_parsec": (_I, [ctypes.c_char_p, _I, ctypes.POINTER(BookC)]),
+    "bsg_parse_parsec": (_I, [ctypes.c_char_p, _SZ, _I, ctypes.POINTER(BookC)]),
+    "bsg_book_free": (None, [ctypes.POINTER(BookC)]),
+    "bsg_write_parsec_prices": (_I, [ctypes.c_char_p, _P, _SZ, _I]),
+    "bsg_format_prices": (_I, [_P, _SZ, _I, ctypes.POINTER(ctypes.c_void_p),
+                               ctypes.POINTER(ctypes.c_size_t)]),
+    "bsg_text_free": (None, [ctypes.c_void_p]),
+    "bsg_write_parsec_input": (_I, [ctypes.c_char_p, ctypes.POINTER(BookC), _I]),
+    "bsg_write_soa": (_I, [ctypes.c_char_p, ctypes.POINTER(BookC)]),
+    "bsg_read_soa": (_I, [ctypes.c_char_p, ctypes.POINTER(BookC)]),
     "bsg_autotune": (_I, [_P, _SZ, ctypes.POINTER(Tune)]),
     "bsg_get_tune": (_I, [_P, ctypes.POINTER(Tune)]),
     "bsg_set_tune": (_I, [_P, ctypes.POINTER(Tune)]),
@@ -408,6 +426,104 @@ def price_batch_noalloc(pool, prices, pool_len, segments, stream=0, asynchronous
     flags = DEVICE_PTRS | (ASYNC if asynchronous else 0)
     return lib.bsg_price_batch_noalloc(*[ptr(x) for x in pool], ptr(prices), pool_len, segs,
                                        len(segments), stream, flags)
+
+
+# ------------------------------------------------------------------ file I/O
+def _book_from_c(b: BookC):
+    from .books import Book
+    n = int(b.n)
+
+    def arr(addr, dt):
+        if n == 0:
+            return np.zeros(0, dtype=dt)
+        raw = (ctypes.c_char * (4 * n)).from_address(addr)
+        return np.frombuffer(raw, dtype=dt).copy()
+    book = Book(arr(b.sptprice, np.float32), arr(b.strike, np.float32), arr(b.rate, np.float32),
+                arr(b.volatility, np.float32), arr(b.otime, np.float32), arr(b.otype, np.int32))
+    return book, arr(b.dgrefval, np.float32)
+
+
+def read_parsec(path, nthreads: int = 0):
+    """bsg_read_parsec: (Book, dgrefval) from a PARSEC input file."""
+    lib = load()
+    b = BookC()
+    st = lib.bsg_read_parsec(os.fsencode(path), nthreads, ctypes.byref(b))
+    if st != 0:
+        raise BsgError(st, f"cannot read {path}")
+    try:
+        return _book_from_c(b)
+    finally:
+        lib.bsg_book_free(ctypes.byref(b))
+
+
+def parse_parsec(text: bytes, nthreads: int = 0):
+    lib = load()
+    b = BookC()
+    st = lib.bsg_parse_parsec(text, len(text), nthreads, ctypes.byref(b))
+    if st != 0:
+        raise BsgError(st, "cannot parse PARSEC text")
+    try:
+        return _book_from_c(b)
+    finally:
+        lib.bsg_book_free(ctypes.byref(b))
+
+
+def format_prices(prices, nthreads: int = 0) -> bytes:
+    """bsg_format_prices: the reference's output file as bytes."""
+    lib = load()
+    p = np.ascontiguousarray(prices, dtype=np.float32)
+    text = ctypes.c_void_p()
+    ln = ctypes.c_size_t()
+    st = lib.bsg_format_prices(ptr(p), len(p), nthreads, ctypes.byref(text), ctypes.byref(ln))
+    if st != 0:
+        raise BsgError(st, "format failed")
+    try:
+        return ctypes.string_at(text.value, ln.value)
+    finally:
+        lib.bsg_text_free(text)
+
+
+def write_parsec_prices(path, prices, nthreads: int = 0):
+    lib = load()
+    p = np.ascontiguousarray(prices, dtype=np.float32)
+    st = lib.bsg_write_parsec_prices(os.fsencode(path), ptr(p), len(p), nthreads)
+    if st != 0:
+        raise BsgError(st, f"cannot write {path}")
+
+
+def write_parsec_input(path, book, dgrefval=None, nthreads: int = 0):
+    """bsg_write_parsec_input: a PARSEC input file from a Book (parallel)."""
+    lib = load()
+    n = len(book)
+    arrs = [np.ascontiguousarray(a) for a in book.arrays()]
+    dg = None if dgrefval is None else np.ascontiguousarray(dgrefval, np.float32)
+    b = BookC(n, *[ptr(a) for a in arrs], ptr(dg) if dg is not None else None, None)
+    st = lib.bsg_write_parsec_input(os.fsencode(path), ctypes.byref(b), nthreads)
+    if st != 0:
+        raise BsgError(st, f"cannot write {path}")
+
+
+def write_soa(path, book, dgrefval=None):
+    lib = load()
+    n = len(book)
+    arrs = [np.ascontiguousarray(a) for a in book.arrays()]
+    dg = np.zeros(n, np.float32) if dgrefval is None else np.ascontiguousarray(dgrefval, np.float32)
+    b = BookC(n, *[ptr(a) for a in arrs], ptr(dg), None)
+    st = lib.bsg_write_soa(os.fsencode(path), ctypes.byref(b))
+    if st != 0:
+        raise BsgError(st, f"cannot write {path}")
+
+
+def read_soa(path):
+    lib = load()
+    b = BookC()
+    st = lib.bsg_read_soa(os.fsencode(path), ctypes.byref(b))
+    if st != 0:
+        raise BsgError(st, f"cannot read {path}")
+    try:
+        return _book_from_c(b)
+    finally:
+        lib.bsg_book_free(ctypes.byref(b))
 
 
 def BlkSchlsEqEuroNoDiv(OptionPrice, numOptions, sptprice, strike, rate, volatility,

@@ -25,6 +25,9 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-Wall", "-I" + os.path.join(ROOT, "include"),
                      "-I" + CSRC]
 CU_SOURCES = ["bsg_kernels.cu", "bsg_api.cu", "bsg_serve.cu", "bsg_noalloc.cu"]
+CPP_SOURCES = ["bsg_io.cpp"]  # host code, compiled with g++
+CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-pthread",
+             "-I" + os.path.join(ROOT, "include")]
 
 
 def nvcc() -> str:
@@ -68,13 +71,21 @@ def build(verbose: bool = False, force: bool = False) -> str:
         objs.append(o)
         if force or _stale(o, [s] + heads):
             jobs.append([nv] + NVCC_FLAGS + ["-c", s, "-o", o])
+    for src in CPP_SOURCES:
+        s = os.path.join(CSRC, src)
+        if not os.path.exists(s):
+            continue
+        o = os.path.join(BUILD, src.replace(".cpp", ".o"))
+        objs.append(o)
+        if force or _stale(o, [s] + heads):
+            jobs.append(["g++"] + CXX_FLAGS + ["-c", s, "-o", o])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
             for out in ex.map(_run, jobs):
                 if verbose and out.strip():
                     print(out)
     if force or jobs or _stale(LIB, objs):
-        _run([nv] + ARCH + ["-shared", "-o", LIB] + objs)
+        _run([nv] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"])
     cli_src = os.path.join(HOST, "blackscholes_gpu.cpp")
     if os.path.exists(cli_src) and (force or _stale(CLI, [cli_src, LIB] + heads)):
         os.makedirs(os.path.dirname(CLI), exist_ok=True)

@@ -25,13 +25,8 @@
 #define fptype float
 #define NUM_RUNS BSG_NUM_RUNS
 
-typedef struct OptionData_ {  // blackscholes.c:89-100
-    fptype s, strike, r, divq, v, t;
-    char OptionType;
-    fptype divs, DGrefval;
-} OptionData;
-
-static OptionData* data;
+// OptionData (blackscholes.c:89-100) is the parsed bsg_book: the five SoA
+// arrays, otype and the DGrefval column (divq and divs are unused).
 static fptype* prices;
 static int numOptions;
 static int* otype;
@@ -85,39 +80,25 @@ int main(int argc, char** argv) {
     }
     const bool errChk = getenv("BSG_ERR_CHK") && atoi(getenv("BSG_ERR_CHK")) != 0;
 
-    FILE* file = fopen(inputFile, "r");
-    if (file == NULL) {
-        printf("ERROR: Unable to open file `%s'.\n", inputFile);
-        exit(1);
+    // Parse in parallel with the reference's field conversions
+    // (blackscholes.c:695-739); bsg_read_parsec fails where fscanf would.
+    bsg_book book;
+    {
+        FILE* probe = fopen(inputFile, "r");
+        if (probe == NULL) {
+            printf("ERROR: Unable to open file `%s'.\n", inputFile);
+            exit(1);
+        }
+        fclose(probe);
     }
-    if (fscanf(file, "%i", &numOptions) != 1 || numOptions < 0) {
+    if (bsg_read_parsec(inputFile, 0, &book) != BSG_OK) {
         printf("ERROR: Unable to read from file `%s'.\n", inputFile);
-        fclose(file);
         exit(1);
     }
+    numOptions = (int)book.n;
     if (nThreads > numOptions) {
         printf("WARNING: Not enough work, reducing number of threads to match number of options.\n");
         nThreads = numOptions;
-    }
-    data = (OptionData*)malloc(sizeof(OptionData) * (size_t)(numOptions ? numOptions : 1));
-    prices = (fptype*)bsg_host_alloc(sizeof(fptype) * (size_t)(numOptions ? numOptions : 1));
-    if (!data || !prices) {
-        printf("ERROR: out of memory\n");
-        exit(1);
-    }
-    for (int i = 0; i < numOptions; ++i) {
-        int rv = fscanf(file, "%f %f %f %f %f %f %c %f %f", &data[i].s, &data[i].strike,
-                        &data[i].r, &data[i].divq, &data[i].v, &data[i].t,
-                        &data[i].OptionType, &data[i].divs, &data[i].DGrefval);
-        if (rv != 9) {
-            printf("ERROR: Unable to read from file `%s'.\n", inputFile);
-            fclose(file);
-            exit(1);
-        }
-    }
-    if (fclose(file) != 0) {
-        printf("ERROR: Unable to close file `%s'.\n", inputFile);
-        exit(1);
     }
     printf("Num of Options: %d\n", numOptions);
     printf("Num of Runs: %d\n", numRuns);
@@ -125,9 +106,10 @@ int main(int argc, char** argv) {
     // SoA in pinned memory (blackscholes.c:747-767 layout: one buffer of 5N
     // floats, otype separate)
     const size_t n = (size_t)numOptions;
+    prices = (fptype*)bsg_host_alloc(sizeof(fptype) * (n ? n : 1));
     fptype* buffer = (fptype*)bsg_host_alloc(5 * sizeof(fptype) * (n ? n : 1));
     otype = (int*)bsg_host_alloc(sizeof(int) * (n ? n : 1));
-    if (!buffer || !otype) {
+    if (!buffer || !otype || !prices) {
         printf("ERROR: out of pinned memory\n");
         exit(1);
     }
@@ -136,15 +118,17 @@ int main(int argc, char** argv) {
     rate = strike + n;
     volatility = rate + n;
     otime = volatility + n;
-    for (size_t i = 0; i < n; ++i) {
-        otype[i] = (data[i].OptionType == 'P') ? 1 : 0;
-        sptprice[i] = data[i].s;
-        strike[i] = data[i].strike;
-        rate[i] = data[i].r;
-        volatility[i] = data[i].v;
-        otime[i] = data[i].t;
+    if (n) {
+        memcpy(sptprice, book.sptprice, n * sizeof(fptype));
+        memcpy(strike, book.strike, n * sizeof(fptype));
+        memcpy(rate, book.rate, n * sizeof(fptype));
+        memcpy(volatility, book.volatility, n * sizeof(fptype));
+        memcpy(otime, book.otime, n * sizeof(fptype));
+        memcpy(otype, book.otype, n * sizeof(int));
     }
-    printf("Size of data: %zu\n", n * (sizeof(OptionData) + sizeof(int)));
+    // the reference prints numOptions * (sizeof(OptionData) + sizeof(int)),
+    // with sizeof(OptionData) = 36 (8 floats and a padded char)
+    printf("Size of data: %zu\n", n * (36 + sizeof(int)));
 
     int st = bsg_create(&ctx, 0, n ? n : 1);
     if (st != BSG_OK) {
@@ -162,34 +146,19 @@ int main(int argc, char** argv) {
 
     if (errChk) {
         for (size_t i = 0; i < n; ++i) {
-            const fptype priceDelta = data[i].DGrefval - prices[i];
+            const fptype priceDelta = book.dgrefval[i] - prices[i];
             if (fabs(priceDelta) >= 1e-4) {
                 printf("Error on %zu. Computed=%.5f, Ref=%.5f, Delta=%.5f\n", i, prices[i],
-                       data[i].DGrefval, priceDelta);
+                       book.dgrefval[i], priceDelta);
                 numError++;
             }
         }
     }
 
-    file = fopen(outputFile, "w");
-    if (file == NULL) {
-        printf("ERROR: Unable to open file `%s'.\n", outputFile);
-        exit(1);
-    }
-    if (fprintf(file, "%i\n", numOptions) < 0) {
+    // "%i\n" then "%.18f\n" per price, formatted in parallel, byte-identical
+    // to the reference's fprintf (blackscholes.c:923-947)
+    if (bsg_write_parsec_prices(outputFile, prices, n, 0) != BSG_OK) {
         printf("ERROR: Unable to write to file `%s'.\n", outputFile);
-        fclose(file);
-        exit(1);
-    }
-    for (size_t i = 0; i < n; ++i) {
-        if (fprintf(file, "%.18f\n", prices[i]) < 0) {
-            printf("ERROR: Unable to write to file `%s'.\n", outputFile);
-            fclose(file);
-            exit(1);
-        }
-    }
-    if (fclose(file) != 0) {
-        printf("ERROR: Unable to close file `%s'.\n", outputFile);
         exit(1);
     }
     if (errChk) printf("Num Errors: %d\n", numError);
@@ -197,6 +166,6 @@ int main(int argc, char** argv) {
     bsg_host_free(buffer);
     bsg_host_free(otype);
     bsg_host_free(prices);
-    free(data);
+    bsg_book_free(&book);
     return 0;
 }
