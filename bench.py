@@ -501,6 +501,62 @@ def run_serve(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+# --------------------------------------------------------- FP64 product mode
+def run_fp64(args, rank, world, local):
+    """The FP64 product mode (double storage, the SIMD variant's NCO = 2
+    types): options/s of num_runs passes, and the roofline that binds it."""
+    import torch
+
+    import oracle
+    from p3arsec_gb300 import Context, books
+    from p3arsec_gb300 import build as b
+    b.build()
+    torch.cuda.set_device(local)
+    n, runs = args.n, args.runs
+    book = books.generate(n, seed=SEED + 8)
+    dev = [torch.from_numpy(a).to(f"cuda:{local}") for a in oracle.widened(book)]
+    ot = torch.from_numpy(book.otype).to(f"cuda:{local}")
+    out = torch.empty(n, dtype=torch.float64, device=f"cuda:{local}")
+    ctx = Context(local, max_options=1)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{local}")
+
+    def step():
+        ctx.price_soa_f64(*dev, ot, out, n=n, num_runs=runs, device=True, asynchronous=True)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    l0 = ctx.launches
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        e1.synchronize()
+    secs = e0.elapsed_time(e1) / 1e3
+    sample = np.random.default_rng(1).choice(n, min(n, 200000), replace=False)
+    got = out.cpu().numpy()[sample]
+    want = oracle.price_fp64(book.slice(0, n))[sample] if n <= (1 << 22) else None
+    value = n * runs * args.steps / secs
+    line = {"metric": "FP64 product mode: options/s (double storage)", "value": value, "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True, "dtype": "f64",
+            "data": "synthetic (seeded book widened to double)",
+            "config": {"workload": f"FP64 map, {n} options, {runs} passes per step",
+                       "options": n, "num_runs": runs},
+            "roofline": {"bound": "fp64 issue", "achieved_GBps": 52 * value / 1e9,
+                         "note": "52 B/option would allow ~1.3e11 options/s from HBM; "
+                                 "GB300's FP64 rate binds first"},
+            "max_rel_vs_cpu_fp64": (float(np.max(np.abs(got - want) / np.maximum(np.abs(want), 1e-300)))
+                                    if want is not None else None),
+            "gpu_launches": ctx.launches - l0, "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 # ---------------------------------------------------------------- file I/O
 def run_io(args, rank, world, local):
     """The reference's file formats: parallel parse / write of libbsgpu.so vs
@@ -612,7 +668,8 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=["map", "batch", "precision", "serve", "io"], default="map")
+    ap.add_argument("--config", choices=["map", "batch", "precision", "serve", "io", "fp64"],
+                    default="map")
     ap.add_argument("--serve-rate", type=float, default=20000.0)
     ap.add_argument("--serve-rates",
                     default="1000,5000,10000,15000,20000,30000,40000,50000,60000,70000,80000")
@@ -639,6 +696,8 @@ def main(argv=None):
         run_serve(args, rank, world, local)
     elif args.config == "io":
         run_io(args, rank, world, local)
+    elif args.config == "fp64":
+        run_fp64(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 

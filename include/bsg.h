@@ -97,6 +97,16 @@ int bsg_BlkSchlsEqEuroNoDiv(float* OptionPrice, int numOptions, float* sptprice,
                             float* strike, float* rate, float* volatility,
                             float* time, int* otype, float timet);
 
+/* FP64 product mode: double storage in and out, the types of the
+ * reference's SIMD variant built with NCO = 2 (blackscholes.simd.c:68-81,
+ * 221-298), num_runs passes.  Bound by the GPU's FP64 rate.  Host or device
+ * pointers as bsg_price_soa (host calls stage through temporary device
+ * memory). */
+int bsg_price_soa_f64(bsg_ctx* ctx, const double* sptprice, const double* strike,
+                      const double* rate, const double* volatility,
+                      const double* otime, const int32_t* otype, double* prices,
+                      size_t n, int num_runs, unsigned flags);
+
 /* FP64 evaluation of the same formula (validation oracle kernel).  Same
  * pointer rules as bsg_price_soa; out is double. */
 int bsg_price_fp64(bsg_ctx* ctx, const float* sptprice, const float* strike,

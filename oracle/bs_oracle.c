@@ -309,3 +309,13 @@ int bso_write_prices_fprintf(const char* path, const float* prices, size_t n)
         }
     return fclose(f) == 0 ? 0 : -1;
 }
+
+/* FP64 over double inputs: the storage of the SIMD variant's NCO = 2 build
+ * (blackscholes.simd.c:68-81) */
+void bso_price_fp64_soa_d(size_t n, const double* s, const double* k, const double* r,
+                          const double* v, const double* t, const int32_t* otype,
+                          double* prices)
+{
+    for (size_t i = 0; i < n; ++i)
+        prices[i] = bso_price_fp64(s[i], k[i], r[i], v[i], t[i], otype[i]);
+}

@@ -47,6 +47,11 @@ void bso_price_fp64_soa(size_t n, const float* s, const float* k, const float* r
                         const float* v, const float* t, const int32_t* otype,
                         double* prices);
 
+/* The FP64 formula over double inputs (the SIMD variant's NCO = 2 storage). */
+void bso_price_fp64_soa_d(size_t n, const double* s, const double* k, const double* r,
+                          const double* v, const double* t, const int32_t* otype,
+                          double* prices);
+
 /* Static block partition of [0, n) over nw workers, as FastFlow's default
  * static scheduling does (ff/parallel_for_internals.hpp:498-519): nw
  * contiguous blocks of floor(n/nw) options, the first n % nw blocks one

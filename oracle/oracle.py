@@ -21,6 +21,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "libbsoracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libbsref.so")
+REF_SIMD_SO = {4: os.path.join(HERE, "_ref", "libbsref_simd4.so"),
+               2: os.path.join(HERE, "_ref", "libbsref_simd2.so")}
 REF_SRC = os.path.join("/root/reference", "parsec-ff", "pkgs", "apps", "blackscholes",
                        "src", "blackscholes.c")
 
@@ -57,6 +59,8 @@ def lib() -> ctypes.CDLL:
         L.bso_price_ref_soa.argtypes = [ctypes.c_size_t] + [_P] * 7
         L.bso_price_fp64_soa.restype = None
         L.bso_price_fp64_soa.argtypes = [ctypes.c_size_t] + [_P] * 7
+        L.bso_price_fp64_soa_d.restype = None
+        L.bso_price_fp64_soa_d.argtypes = [ctypes.c_size_t] + [_P] * 7
         L.bso_static_partition.restype = None
         L.bso_static_partition.argtypes = [ctypes.c_int64, ctypes.c_int, _P, _P]
         L.bso_read_parsec_fscanf.restype = ctypes.c_long
@@ -121,6 +125,48 @@ def price_reference(book):
     a = _arrs(book)
     out = np.empty(len(book), dtype=np.float32)
     R.bsref_price_soa(len(book), *[_p(x) for x in a], _p(out))
+    return out
+
+
+def widened(book):
+    """The book's five float arrays widened to double (NCO = 2 storage)."""
+    return [np.ascontiguousarray(a, dtype=np.float64) for a in book.arrays()[:5]]
+
+
+def price_fp64_d(s, k, r, v, t, otype) -> np.ndarray:
+    """FP64 formula over double inputs."""
+    a = [np.ascontiguousarray(x, dtype=np.float64) for x in (s, k, r, v, t)]
+    ot = np.ascontiguousarray(otype, dtype=np.int32)
+    out = np.empty(len(ot), dtype=np.float64)
+    lib().bso_price_fp64_soa_d(len(ot), *[_p(x) for x in a], _p(ot), _p(out))
+    return out
+
+
+_simd = {}
+
+
+def price_reference_simd(book, nco: int):
+    """The reference's SIMD variant (blackscholes.simd.c:221-298) in packets of
+    nco: 4 = SSE float on the float inputs, 2 = SSE2 double on the inputs
+    widened to double.  None where it was not built (non-x86 machines)."""
+    if nco not in _simd:
+        path = REF_SIMD_SO[nco]
+        if not os.path.exists(path):
+            return None
+        L = ctypes.CDLL(path)
+        fn = getattr(L, f"bsref_simd{nco}_price")
+        fn.restype = None
+        fn.argtypes = [ctypes.c_size_t] + [_P] * 7
+        _simd[nco] = fn
+    fn = _simd[nco]
+    ot = np.ascontiguousarray(book.otype, dtype=np.int32)
+    if nco == 4:
+        a = _arrs(book)[:5]
+        out = np.empty(len(book), dtype=np.float32)
+    else:
+        a = widened(book)
+        out = np.empty(len(book), dtype=np.float64)
+    fn(len(book), *[_p(x) for x in a], _p(ot), _p(out))
     return out
 
 

@@ -134,6 +134,7 @@ SIGNATURES = {
     "bsg_price_soa": (_I, [_P] + [_P] * 7 + [_SZ, _I, _U]),
     "bsg_BlkSchlsEqEuroNoDiv": (_I, [_P, _I] + [_P] * 6 + [ctypes.c_float]),
     "bsg_price_fp64": (_I, [_P] + [_P] * 7 + [_SZ, _U]),
+    "bsg_price_soa_f64": (_I, [_P] + [_P] * 7 + [_SZ, _I, _U]),
     "bsg_price_batch": (_I, [_P] + [_P] * 7 + [_SZ, ctypes.POINTER(Segment), _SZ, _I, _U]),
     "bsg_price_books_plain": (_I, [_P] + [_P] * 7 + [_SZ, ctypes.POINTER(Segment), _SZ, _I, _U]),
     "bsg_price_batch_noalloc": (_I, [_P] * 7 + [_SZ, ctypes.POINTER(Segment), _SZ, _P, _U]),
@@ -279,6 +280,17 @@ class Context:
                                      ptr(out), n, flags)
         _check(self.lib, self.h, st)
         return out
+
+    def price_soa_f64(self, s, k, r, v, t, otype, prices, n=None, num_runs=1, device=False,
+                      asynchronous=False):
+        """FP64 product mode: double arrays in, double prices out."""
+        if n is None:
+            n = len(s)
+        flags = (DEVICE_PTRS if device else HOST_PTRS) | (ASYNC if asynchronous else 0)
+        st = self.lib.bsg_price_soa_f64(self.h, ptr(s), ptr(k), ptr(r), ptr(v), ptr(t),
+                                        ptr(otype), ptr(prices), n, num_runs, flags)
+        _check(self.lib, self.h, st)
+        return prices
 
     def price_batch(self, pool, prices, pool_len, segments, num_runs=1, mode="fast",
                     plain=False, asynchronous=False, graph=True):

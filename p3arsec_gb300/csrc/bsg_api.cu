@@ -530,6 +530,57 @@ int bsg_price_fp64(bsg_ctx* c, const float* s, const float* k, const float* r,
     return BSG_OK;
 }
 
+int bsg_price_soa_f64(bsg_ctx* c, const double* s, const double* k, const double* r,
+                      const double* v, const double* t, const int32_t* otype, double* prices,
+                      size_t n, int num_runs, unsigned flags) {
+    if (!c) return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (num_runs < 0 || (flags & ~(BSG_DEVICE_PTRS | BSG_ASYNC | BSG_NO_GRAPH)))
+        return fail(c, BSG_ERR_INVALID_ARG, "bad flags or num_runs");
+    if (n == 0 || num_runs == 0) return BSG_OK;
+    if (n > ((size_t)1 << 36)) return fail(c, BSG_ERR_INVALID_ARG, "n too large");
+    BSG_CK(c, cudaSetDevice(c->device));
+    int st;
+    if (flags & BSG_DEVICE_PTRS) {
+        const size_t b = n * 8;
+        if ((st = check_dev_range(c, s, b, "sptprice")) || (st = check_dev_range(c, k, b, "strike")) ||
+            (st = check_dev_range(c, r, b, "rate")) || (st = check_dev_range(c, v, b, "volatility")) ||
+            (st = check_dev_range(c, t, b, "otime")) || (st = check_dev_range(c, otype, n * 4, "otype")) ||
+            (st = check_dev_range(c, prices, b, "prices")))
+            return st;
+        const bsg::SoA64 a{s, k, r, v, t, otype, prices};
+        for (int j = 0; j < num_runs; ++j) {
+            cudaError_t e = bsg::launch_map_f64(a, (int64_t)n, c->sm_count, c->stream);
+            if (e != cudaSuccess) return cuda_fail(c, e, "launch_map_f64");
+            c->launches++;
+        }
+        return finish(c, flags);
+    }
+    if (flags & BSG_ASYNC) return fail(c, BSG_ERR_INVALID_ARG, "BSG_ASYNC needs device pointers");
+    if (!s || !k || !r || !v || !t || !otype || !prices)
+        return fail(c, BSG_ERR_INVALID_ARG, "a host array is NULL");
+    // host arrays: a temporary device copy (this mode has no resident buffers)
+    const size_t al = round_up(n, 32);
+    char* buf = nullptr;
+    BSG_CK(c, cudaMalloc(&buf, al * (6 * 8 + 4)));
+    std::unique_ptr<char, decltype(&cudaFree)> guard(buf, &cudaFree);
+    double* d = reinterpret_cast<double*>(buf);
+    int32_t* dot = reinterpret_cast<int32_t*>(d + 6 * al);
+    const double* src[5] = {s, k, r, v, t};
+    for (int j = 0; j < 5; ++j)
+        BSG_CK(c, cudaMemcpyAsync(d + j * al, src[j], n * 8, cudaMemcpyHostToDevice, c->stream));
+    BSG_CK(c, cudaMemcpyAsync(dot, otype, n * 4, cudaMemcpyHostToDevice, c->stream));
+    const bsg::SoA64 a{d, d + al, d + 2 * al, d + 3 * al, d + 4 * al, dot, d + 5 * al};
+    for (int j = 0; j < num_runs; ++j) {
+        cudaError_t e = bsg::launch_map_f64(a, (int64_t)n, c->sm_count, c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "launch_map_f64");
+        c->launches++;
+    }
+    BSG_CK(c, cudaMemcpyAsync(prices, d + 5 * al, n * 8, cudaMemcpyDeviceToHost, c->stream));
+    BSG_CK(c, cudaStreamSynchronize(c->stream));
+    return BSG_OK;
+}
+
 int bsg_price_batch(bsg_ctx* c, const float* s, const float* k, const float* r,
                     const float* v, const float* t, const int32_t* otype,
                     float* prices, size_t pool_len, const bsg_segment* segs,

@@ -20,6 +20,17 @@ struct SoA {
     float* out;
 };
 
+// The FP64 product mode's SoA: double storage (otype int32).
+struct SoA64 {
+    const double* s;
+    const double* k;
+    const double* r;
+    const double* v;
+    const double* t;
+    const int32_t* ot;
+    double* out;
+};
+
 // Plain-map launch shape (see bsg_tune in bsg.h).
 struct MapCfg {
     int vpt;           // vector groups per thread per tile: 1, 2, 4
@@ -51,6 +62,8 @@ bool map_vectorizable(const SoA& a, const MapCfg& cfg);
 
 cudaError_t launch_fp64(const SoA& a, double* out, int64_t n, int sm_count,
                         cudaStream_t st);
+// One pass of the FP64 product mode over n options.
+cudaError_t launch_map_f64(const SoA64& a, int64_t n, int sm_count, cudaStream_t st);
 
 // Persistent batched pricing.  seg_off/seg_len/tile_prefix are device arrays
 // of nseg (tile_prefix: nseg + 1 entries, exclusive prefix of tiles of

@@ -243,6 +243,24 @@ __global__ void __launch_bounds__(256) fp64_kernel(SoA a, double* out, int64_t n
         out[i] = price_fp64(a.s[i], a.k[i], a.r[i], a.v[i], a.t[i], a.ot[i]);
 }
 
+// FP64 product mode: double storage in and out (the SIMD variant's NCO = 2
+// types), 52 bytes per option; bound by GB300's FP64 rate, not by HBM.
+__global__ void __launch_bounds__(256) map_f64_kernel(SoA64 a, int64_t n) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        a.out[i] = price_fp64(__ldg(a.s + i), __ldg(a.k + i), __ldg(a.r + i), __ldg(a.v + i),
+                              __ldg(a.t + i), __ldg(a.ot + i));
+}
+
+cudaError_t launch_map_f64(const SoA64& a, int64_t n, int sm_count, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    int64_t grid = (n + 255) / 256;
+    const int64_t cap = (int64_t)sm_count * 8;
+    if (grid > cap) grid = cap;
+    map_f64_kernel<<<(unsigned)grid, 256, 0, st>>>(a, n);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_fp64(const SoA& a, double* out, int64_t n, int sm_count,
                         cudaStream_t st) {
     if (n <= 0) return cudaSuccess;

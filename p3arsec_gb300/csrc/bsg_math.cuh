@@ -281,33 +281,42 @@ __device__ __forceinline__ float price_libm_ref(float s, float k, float r, float
 }
 
 // ------------------------------------------------------------------- FP64
+// The same formula in double, operation for operation as the reference's
+// NCO = 2 SIMD build evaluates it (blackscholes.simd.c:134-298), with
+// explicitly rounded operations (no fused multiply-adds): only CUDA's double
+// exp/log can differ from the host libm's, by an ulp.
 __device__ __forceinline__ double cndf_fp64(double x) {
     const bool neg = x < 0.0;
     x = neg ? -x : x;
-    const double np = exp(-0.5 * x * x) * BSG_INV_SQRT_2PI;
-    const double k = 1.0 / (1.0 + BSG_C0 * x);
-    const double k2 = k * k, k3 = k2 * k, k4 = k3 * k, k5 = k4 * k;
+    const double np = __dmul_rn(exp(__dmul_rn(__dmul_rn(-0.5, x), x)), BSG_INV_SQRT_2PI);
+    const double k = __ddiv_rn(1.0, __dadd_rn(1.0, __dmul_rn(BSG_C0, x)));
+    const double k2 = __dmul_rn(k, k), k3 = __dmul_rn(k2, k);
+    const double k4 = __dmul_rn(k3, k), k5 = __dmul_rn(k4, k);
     double l2 = __dadd_rn(__dmul_rn(k2, BSG_C2), __dmul_rn(k3, BSG_C3));
     l2 = __dadd_rn(l2, __dmul_rn(k4, BSG_C4));
     l2 = __dadd_rn(l2, __dmul_rn(k5, BSG_C5));
     const double l1 = __dadd_rn(l2, __dmul_rn(k, BSG_C1));
-    const double out = 1.0 - l1 * np;
-    return neg ? 1.0 - out : out;
+    const double out = __dsub_rn(1.0, __dmul_rn(l1, np));
+    return neg ? __dsub_rn(1.0, out) : out;
 }
 
 __device__ __forceinline__ double d1_fp64(double s, double k, double r, double v, double t) {
-    return ((r + v * v * 0.5) * t + log(s / k)) / (v * sqrt(t));
+    const double num = __dadd_rn(__dmul_rn(__dadd_rn(r, __dmul_rn(__dmul_rn(v, v), 0.5)), t),
+                                 log(__ddiv_rn(s, k)));
+    return __ddiv_rn(num, __dmul_rn(v, __dsqrt_rn(t)));
 }
 
 __device__ __forceinline__ double price_fp64(double s, double k, double r, double v,
                                              double t, int otype) {
-    const double den = v * sqrt(t);
-    const double d1 = ((r + v * v * 0.5) * t + log(s / k)) / den;
-    const double d2 = d1 - den;
+    const double den = __dmul_rn(v, __dsqrt_rn(t));
+    const double num = __dadd_rn(__dmul_rn(__dadd_rn(r, __dmul_rn(__dmul_rn(v, v), 0.5)), t),
+                                 log(__ddiv_rn(s, k)));
+    const double d1 = __ddiv_rn(num, den);
+    const double d2 = __dsub_rn(d1, den);
     const double n1 = cndf_fp64(d1), n2 = cndf_fp64(d2);
-    const double fv = k * exp(-r * t);
-    if (otype == 0) return s * n1 - fv * n2;
-    return fv * (1.0 - n2) - s * (1.0 - n1);
+    const double fv = __dmul_rn(k, exp(__dmul_rn(-r, t)));
+    if (otype == 0) return __dsub_rn(__dmul_rn(s, n1), __dmul_rn(fv, n2));
+    return __dsub_rn(__dmul_rn(fv, __dsub_rn(1.0, n2)), __dmul_rn(s, __dsub_rn(1.0, n1)));
 }
 
 template <int M>

@@ -72,18 +72,26 @@ def run_cli(binary, nthreads, inp, out):
 
 def main():
     oracle.build(ref=True)
-    if oracle.ref_lib() is None:
-        raise SystemExit("the reference could not be built (source tree absent?)")
+    if oracle.ref_lib() is None or oracle.price_reference_simd(CASES["edge"](), 2) is None:
+        raise SystemExit("the reference could not be built (source tree absent, or not x86-64)")
     meta = {}
     for name, make in CASES.items():
         book = make()
         ref = oracle.price_reference(book)
         fp64 = oracle.price_fp64(book)
+        # the reference's SIMD variant (blackscholes.simd.c): NCO = 4 (SSE
+        # float) and NCO = 2 (SSE2 double, inputs widened to double)
+        simd4 = oracle.price_reference_simd(book, 4)
+        simd2 = oracle.price_reference_simd(book, 2)
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"),
                             sptprice=book.sptprice, strike=book.strike, rate=book.rate,
                             volatility=book.volatility, otime=book.otime, otype=book.otype,
-                            ref_prices=ref, fp64_prices=fp64)
-        info = {"n": len(book), "cli": {}}
+                            ref_prices=ref, fp64_prices=fp64, simd4_prices=simd4,
+                            simd2_prices=simd2)
+        info = {"n": len(book), "cli": {},
+                "simd2_equals_fp64_oracle_bitwise": bool(np.array_equal(
+                    simd2.view(np.uint64), fp64.view(np.uint64))),
+                "simd4_vs_scalar_max_abs": float(np.abs(simd4.astype(np.float64) - ref).max())}
         with tempfile.TemporaryDirectory() as td:
             inp = os.path.join(td, "in.txt")
             books.write_parsec_input(inp, book, dgrefval=fp64)

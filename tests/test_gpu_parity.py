@@ -166,3 +166,39 @@ def test_reference_batch_signature(gpu_ctx):
     out = np.zeros(len(book), dtype=np.float32)
     BlkSchlsEqEuroNoDiv(out, len(book), *book.arrays(), 0.0)
     assert np.abs(out - fp64).max() <= 1e-4
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp64_product_mode_tracks_reference_simd_double(gpu_ctx, name):
+    import os
+    import oracle
+    from conftest import GOLDEN
+    z = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    book, _, _ = load_golden(name)
+    wide = oracle.widened(book)
+    out = np.zeros(len(book), dtype=np.float64)
+    gpu_ctx.price_soa_f64(*wide, book.otype, out, num_runs=3)
+    np.testing.assert_allclose(out, z["simd2_prices"], rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize("name", ["plain_4096", "edge"])
+def test_fast_vs_reference_simd_float(gpu_ctx, name):
+    import os
+    from conftest import GOLDEN
+    z = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    book, _, _ = load_golden(name)
+    got = gpu_ctx.price_book(book)
+    assert np.abs(got.astype(np.float64) - z["simd4_prices"]).max() <= 2e-4
+
+
+def test_fp64_product_mode_device_pointers(gpu_ctx):
+    torch = pytest.importorskip("torch")
+    import oracle
+    book = books.generate(100003, seed=17, dist="tails")
+    wide = [torch.from_numpy(a).cuda() for a in oracle.widened(book)]
+    ot = torch.from_numpy(book.otype).cuda()
+    out = torch.empty(len(book), dtype=torch.float64, device="cuda:0")
+    gpu_ctx.price_soa_f64(*wide, ot, out, n=len(book), device=True)
+    torch.cuda.synchronize()
+    want = oracle.price_fp64(book)
+    np.testing.assert_allclose(out.cpu().numpy(), want, rtol=1e-13, atol=1e-13)

@@ -103,3 +103,24 @@ def test_compiled_reference_agrees_when_present(oracle_lib):
         a = oracle_lib.price_reference(book)
         b = oracle_lib.price_ref(book)
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp64_oracle_is_bit_identical_to_reference_simd_double(oracle_lib, name):
+    """The reference's SIMD variant built with NCO = 2 computes the formula in
+    double (blackscholes.simd.c:68-81); the FP64 oracle reproduces it."""
+    import numpy as np
+    z = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    book, _, _ = load_golden(name)
+    got = oracle_lib.price_fp64_d(*oracle_lib.widened(book), book.otype)
+    assert np.array_equal(got.view(np.uint64), z["simd2_prices"].view(np.uint64))
+
+
+def test_reference_simd_variants_agree_when_present(oracle_lib):
+    if oracle_lib.price_reference_simd(books.generate(8, seed=1), 2) is None:
+        pytest.skip("the SIMD variant is built only on x86-64 with the reference tree")
+    book = books.generate(1 << 19, seed=98, dist="tails")
+    s2 = oracle_lib.price_reference_simd(book, 2)
+    assert np.array_equal(s2.view(np.uint64), oracle_lib.price_fp64(book).view(np.uint64))
+    s4 = oracle_lib.price_reference_simd(book, 4)
+    assert np.abs(s4.astype(np.float64) - s2).max() < 1e-3
