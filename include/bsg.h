@@ -338,7 +338,10 @@ typedef struct bsg_tune {
     int block;          /* threads per block: 128, 256 or 512 */
     int blocks_per_sm;  /* grid = blocks_per_sm * SM count; 0 = one block per tile */
     int load_path;      /* 0 = LDG.128 non-coherent, 1 = LDG.128 evict-first,
-                           2 = LDG.256 non-coherent (8 options per load) */
+                           2 = LDG.256 non-coherent (8 options per load),
+                           3 = TMA bulk copies into a 3-stage shared-memory
+                               ring, one CTA per SM (vec_per_thread, block and
+                               blocks_per_sm are then fixed) */
     int pdl;            /* 1 = programmatic dependent launch between passes */
 } bsg_tune;
 

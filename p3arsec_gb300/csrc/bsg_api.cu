@@ -266,10 +266,18 @@ int enqueue_map_runs(bsg_ctx* c, const bsg::SoA& a, int64_t n, int runs, int mod
     return BSG_OK;
 }
 
+// The bulk-staged kernel reports an expired wait in an error word; any call
+// that synchronises checks it.
+int check_bulk_error(bsg_ctx* c) {
+    if (c->tune.load_path == 3 && bsg::bulk_error_take())
+        return fail(c, BSG_ERR_TIMEOUT, "a bulk-copy wait of the staged map kernel expired");
+    return BSG_OK;
+}
+
 int finish(bsg_ctx* c, unsigned flags) {
     if (flags & BSG_ASYNC) return BSG_OK;
     BSG_CK(c, cudaStreamSynchronize(c->stream));
-    return BSG_OK;
+    return check_bulk_error(c);
 }
 
 int grow_seg_scratch(bsg_ctx* c, size_t nseg) {
@@ -465,7 +473,7 @@ int bsg_price_soa(bsg_ctx* c, const float* s, const float* k, const float* r,
         if ((st = enqueue_map_runs(c, d, (int64_t)n, num_runs, mode, flags))) return st;
         BSG_CK(c, cudaMemcpyAsync(prices, d.out, b, cudaMemcpyDeviceToHost, c->stream));
         BSG_CK(c, cudaStreamSynchronize(c->stream));
-        return BSG_OK;
+        return check_bulk_error(c);
     } catch (const std::bad_alloc&) {
         return fail(c, BSG_ERR_OUT_OF_MEMORY, "host allocation failed");
     }
@@ -752,7 +760,7 @@ static bool tune_valid(const bsg_tune* t) {
                         (t->vec_per_thread == 4 && t->load_path != 2);
     const bool blk_ok = t->block == 128 || t->block == 256 || t->block == 512;
     return vpt_ok && blk_ok && t->blocks_per_sm >= 0 && t->blocks_per_sm <= 64 &&
-           t->load_path >= 0 && t->load_path <= 2 && (t->pdl == 0 || t->pdl == 1);
+           t->load_path >= 0 && t->load_path <= 3 && (t->pdl == 0 || t->pdl == 1);
 }
 
 int bsg_set_tune(bsg_ctx* c, const bsg_tune* t) {
@@ -862,6 +870,28 @@ extern "C" int bsg_autotune(bsg_ctx* c, size_t n, bsg_tune* out) {
                         best = t;
                     }
                 }
+    // the TMA bulk-staged kernel: one shape (one CTA per SM), with and without PDL
+    for (int pdl : {0, 1}) {
+        if (e != cudaSuccess) break;
+        const bsg_tune t{1, 256, 0, 3, pdl};
+        const bsg::MapCfg cfg{1, 256, 0, 3, pdl};
+        e = bsg::launch_map(a, (int64_t)n, bsg::MODE_FAST, cfg, c->sm_count, c->stream);
+        if (e != cudaSuccess) break;
+        cudaEventRecord(e0, c->stream);
+        for (int i = 0; i < reps && e == cudaSuccess; ++i)
+            e = bsg::launch_map(a, (int64_t)n, bsg::MODE_FAST, cfg, c->sm_count, c->stream);
+        cudaEventRecord(e1, c->stream);
+        c->launches += reps + 1;
+        if (e != cudaSuccess) break;
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (bsg::bulk_error_take()) continue;  // never pick a shape whose wait expired
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = t;
+        }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (e != cudaSuccess) return cuda_fail(c, e, "autotune launch");

@@ -36,7 +36,8 @@ struct MapCfg {
     int vpt;           // vector groups per thread per tile: 1, 2, 4
     int block;         // threads per block
     int blocks_per_sm; // 0: one block per tile; else grid = blocks_per_sm * SMs
-    int load_path;     // 0: v4 nc; 1: v4 + L2 evict_first; 2: v8 (256-bit) nc
+    int load_path;     // 0: v4 nc; 1: v4 + L2 evict_first; 2: v8 (256-bit) nc;
+                       // 3: TMA bulk copies into a shared-memory ring
     int pdl;           // 1: launch with programmatic stream serialization
 };
 
@@ -57,6 +58,9 @@ constexpr int kBatchBlock = 256;
 // scalar kernel.  Returns the launch error.
 cudaError_t launch_map(const SoA& a, int64_t n, int mode, const MapCfg& cfg,
                        int sm_count, cudaStream_t st);
+// Reads and clears the bulk-staged kernel's error word (non-zero: a bounded
+// wait expired and some tiles were not priced).
+unsigned bulk_error_take();
 // True when launch_map would take the vector path for these pointers.
 bool map_vectorizable(const SoA& a, const MapCfg& cfg);
 

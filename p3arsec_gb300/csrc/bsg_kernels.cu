@@ -154,15 +154,193 @@ __global__ void __launch_bounds__(256) map_scalar_kernel(SoA a, int64_t n) {
         price_scalar<M>(a, i);
 }
 
+// ------------------------------------------------- TMA bulk-staged variant
+// Each persistent CTA streams whole tiles of kBulkTile options through a
+// kBulkStages-deep ring in shared memory: one thread issues six 1D bulk
+// copies (cp.async.bulk, one per input array) per tile, completing on the
+// stage's mbarrier with a transaction count; every thread waits on the
+// barrier, prices 8 options from shared memory and stores them with 256-bit
+// streaming stores.  The stage is refilled after a block barrier and a proxy
+// fence.  Waits are bounded: on expiry the CTA records kErrBulkTimeout in
+// *err, waits (bounded) for its copies in flight and returns.
+constexpr int kBulkThreads = 256;
+constexpr int kBulkTile = kBulkThreads * 8;          // 2048 options per tile
+constexpr int kBulkStages = 3;
+constexpr int kBulkStageBytes = 6 * kBulkTile * 4;   // 48 KB
+constexpr unsigned kErrBulkTimeout = 1u;
+constexpr uint32_t kBulkWaitLimit = 1u << 22;
+
+// Error word of the bulk kernel (kErrBulkTimeout); read and cleared by the
+// host with bulk_error_take().
+__device__ unsigned g_bulk_err;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+    for (uint32_t i = 0; i < kBulkWaitLimit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// One 1D bulk copy of a tile's worth of one array (kBulkTile * 4 bytes,
+// 16-byte aligned at both ends) into shared memory, completing on `bar`.
+__device__ __forceinline__ void bulk_copy(char* dst, const char* src, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        :: "r"(smem_u32(dst)), "l"(src), "r"(kBulkTile * 4), "r"(bar) : "memory");
+}
+
+// Issues the six copies of tile `tile` into stage memory `st` (thread 0).
+__device__ __forceinline__ void bulk_issue(const SoA& a, int64_t tile, char* st, uint32_t bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                 :: "r"(bar), "r"(kBulkStageBytes) : "memory");
+    const size_t off = (size_t)tile * kBulkTile * 4;
+    bulk_copy(st + 0 * kBulkTile * 4, reinterpret_cast<const char*>(a.s) + off, bar);
+    bulk_copy(st + 1 * kBulkTile * 4, reinterpret_cast<const char*>(a.k) + off, bar);
+    bulk_copy(st + 2 * kBulkTile * 4, reinterpret_cast<const char*>(a.r) + off, bar);
+    bulk_copy(st + 3 * kBulkTile * 4, reinterpret_cast<const char*>(a.v) + off, bar);
+    bulk_copy(st + 4 * kBulkTile * 4, reinterpret_cast<const char*>(a.t) + off, bar);
+    bulk_copy(st + 5 * kBulkTile * 4, reinterpret_cast<const char*>(a.ot) + off, bar);
+}
+
+template <int M>
+__global__ void __launch_bounds__(kBulkThreads) map_bulk_kernel(SoA a, int64_t n) {
+    extern __shared__ __align__(128) char smem[];
+    __shared__ __align__(8) unsigned long long bars[kBulkStages];
+    __shared__ int sh_abort;
+    pdl_trigger();
+    const int64_t ntiles = n / kBulkTile;
+    // tiles of this CTA: blockIdx.x + k * gridDim.x
+    const int64_t mine = (ntiles > blockIdx.x) ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kBulkStages; ++s)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&bars[s])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        sh_abort = 0;
+        for (int s = 0; s < kBulkStages && s < mine; ++s)
+            bulk_issue(a, blockIdx.x + (int64_t)s * gridDim.x, smem + s * kBulkStageBytes,
+                       smem_u32(&bars[s]));
+    }
+    __syncthreads();
+    int64_t k = 0;
+    for (; k < mine; ++k) {
+        const int s = (int)(k % kBulkStages);
+        const uint32_t parity = (uint32_t)((k / kBulkStages) & 1);
+        const bool ok = mbar_wait_bounded(smem_u32(&bars[s]), parity);
+        if (!ok) sh_abort = 1;  // benign race: every writer stores 1
+        __syncthreads();
+        if (sh_abort) break;
+        const char* st = smem + s * kBulkStageBytes;
+        const int64_t tile = blockIdx.x + k * gridDim.x;
+        // thread t prices options 4t..4t+3 and 1024+4t..1024+4t+3 of the
+        // tile, so each 128-bit shared load and global store of a warp
+        // covers 512 contiguous bytes (no bank conflicts)
+        float p[2][4];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int o = (4 * threadIdx.x + 1024 * h) * 4;
+            const float4 S = *reinterpret_cast<const float4*>(st + 0 * kBulkTile * 4 + o);
+            const float4 K = *reinterpret_cast<const float4*>(st + 1 * kBulkTile * 4 + o);
+            const float4 R = *reinterpret_cast<const float4*>(st + 2 * kBulkTile * 4 + o);
+            const float4 V = *reinterpret_cast<const float4*>(st + 3 * kBulkTile * 4 + o);
+            const float4 T = *reinterpret_cast<const float4*>(st + 4 * kBulkTile * 4 + o);
+            const int4 O = *reinterpret_cast<const int4*>(st + 5 * kBulkTile * 4 + o);
+            p[h][0] = price<M>(S.x, K.x, R.x, V.x, T.x, O.x);
+            p[h][1] = price<M>(S.y, K.y, R.y, V.y, T.y, O.y);
+            p[h][2] = price<M>(S.z, K.z, R.z, V.z, T.z, O.z);
+            p[h][3] = price<M>(S.w, K.w, R.w, V.w, T.w, O.w);
+        }
+        __syncthreads();  // every thread has read stage s
+        if (threadIdx.x == 0 && k + kBulkStages < mine) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            bulk_issue(a, blockIdx.x + (k + kBulkStages) * gridDim.x,
+                       smem + s * kBulkStageBytes, smem_u32(&bars[s]));
+        }
+        st_group<4>(a.out + tile * kBulkTile + 4 * threadIdx.x, p[0]);
+        st_group<4>(a.out + tile * kBulkTile + 1024 + 4 * threadIdx.x, p[1]);
+    }
+    if (k < mine) {
+        // timed out: record it, let this CTA's copies in flight land (bounded)
+        if (threadIdx.x == 0) {
+            atomicOr(&g_bulk_err, kErrBulkTimeout);
+            for (int64_t q = k; q < mine && q < k + kBulkStages; ++q)
+                mbar_wait_bounded(smem_u32(&bars[q % kBulkStages]),
+                                  (uint32_t)((q / kBulkStages) & 1));
+        }
+        __syncthreads();
+        return;
+    }
+    // options past the last whole tile: the last CTA, one per thread
+    if (blockIdx.x == gridDim.x - 1)
+        for (int64_t i = ntiles * kBulkTile + threadIdx.x; i < n; i += kBulkThreads)
+            price_scalar<M>(a, i);
+    pdl_wait();
+}
+
+size_t bulk_smem_bytes() { return (size_t)kBulkStages * kBulkStageBytes; }
+
+unsigned bulk_error_take() {
+    unsigned v = 0, zero = 0;
+    if (cudaMemcpyFromSymbol(&v, g_bulk_err, sizeof v) != cudaSuccess ||
+        cudaMemcpyToSymbol(g_bulk_err, &zero, sizeof zero) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return v;
+}
+
 static bool aligned(const void* p, uintptr_t al) {
     return (reinterpret_cast<uintptr_t>(p) & (al - 1)) == 0;
 }
 
 bool map_vectorizable(const SoA& a, const MapCfg& cfg) {
-    const uintptr_t al = (cfg.load_path == 2) ? 32 : 16;
+    const uintptr_t al = (cfg.load_path >= 2) ? 32 : 16;
     return aligned(a.s, al) && aligned(a.k, al) && aligned(a.r, al) &&
            aligned(a.v, al) && aligned(a.t, al) && aligned(a.ot, al) &&
            aligned(a.out, al);
+}
+
+template <int M>
+static cudaError_t launch_map_bulk(const SoA& a, int64_t n, const MapCfg& cfg, int sm_count,
+                                  cudaStream_t st) {
+    // opt in to the 144 KB of dynamic shared memory, once per device
+    static unsigned long long opted = 0;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 64 && !(opted & (1ull << dev))) {
+        e = cudaFuncSetAttribute(map_bulk_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)bulk_smem_bytes());
+        if (e != cudaSuccess) return e;
+        opted |= 1ull << dev;
+    }
+    const int64_t ntiles = n / kBulkTile;
+    int64_t grid = (int64_t)sm_count;  // one CTA per SM (144 KB of staging each)
+    if (grid > ntiles) grid = ntiles;
+    if (grid < 1) grid = 1;
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3((unsigned)grid);
+    lc.blockDim = dim3(kBulkThreads);
+    lc.dynamicSmemBytes = bulk_smem_bytes();
+    lc.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    lc.attrs = attr;
+    lc.numAttrs = cfg.pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&lc, map_bulk_kernel<M>, a, n);
 }
 
 template <int M>
@@ -176,6 +354,14 @@ static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg,
         if (grid < 1) grid = 1;
         map_scalar_kernel<M><<<(unsigned)grid, 256, 0, st>>>(a, n);
         return cudaGetLastError();
+    }
+    if (cfg.load_path == 3) {
+        if constexpr (M == MODE_FAST)
+            if (n >= kBulkTile) return launch_map_bulk<M>(a, n, cfg, sm_count, st);
+        MapCfg v8 = cfg;  // too small for a whole tile (or another mode): 256-bit loads
+        v8.load_path = 2;
+        v8.vpt = 1;
+        return launch_map_mode<M>(a, n, v8, sm_count, st);
     }
     const int W = (cfg.load_path == 2) ? 8 : 4;
     const int64_t ngroups = n / W;

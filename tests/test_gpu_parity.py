@@ -125,9 +125,9 @@ def test_all_tunings_give_identical_bits(gpu_ctx):
     base = gpu_ctx.price_book(book)
     saved = gpu_ctx.get_tune()
     try:
-        for lp in (0, 1, 2):
+        for lp in (0, 1, 2, 3):
             for vpt in (1, 2, 4):
-                if lp == 2 and vpt == 4:
+                if lp >= 2 and vpt == 4:
                     continue
                 for block in (128, 256, 512):
                     for bps, pdl in ((0, 0), (4, 0), (0, 1), (4, 1)):
@@ -202,3 +202,20 @@ def test_fp64_product_mode_device_pointers(gpu_ctx):
     torch.cuda.synchronize()
     want = oracle.price_fp64(book)
     np.testing.assert_allclose(out.cpu().numpy(), want, rtol=1e-13, atol=1e-13)
+
+
+@pytest.mark.parametrize("n", [2047, 2048, 2049, 4096 * 152 + 5, 1000003])
+def test_bulk_staged_path_bits_and_tails(gpu_ctx, n):
+    """The TMA bulk-staged kernel (load path 3): whole tiles through the
+    shared-memory ring, the rest per option; sizes below one tile fall back to
+    256-bit loads.  Same bits as the default path."""
+    book = books.generate(n, seed=71)
+    base = gpu_ctx.price_book(book)
+    saved = gpu_ctx.get_tune()
+    try:
+        for pdl in (0, 1):
+            gpu_ctx.set_tune(1, 256, 0, 3, pdl)
+            got = gpu_ctx.price_book(book, num_runs=5)
+            assert np.array_equal(got.view(np.uint32), base.view(np.uint32))
+    finally:
+        gpu_ctx.set_tune(**saved)
