@@ -339,9 +339,10 @@ typedef struct bsg_tune {
     int blocks_per_sm;  /* grid = blocks_per_sm * SM count; 0 = one block per tile */
     int load_path;      /* 0 = LDG.128 non-coherent, 1 = LDG.128 evict-first,
                            2 = LDG.256 non-coherent (8 options per load),
-                           3 = TMA bulk copies into a 3-stage shared-memory
-                               ring, one CTA per SM (vec_per_thread, block and
-                               blocks_per_sm are then fixed) */
+                           3, 4, 5 = TMA bulk copies into a shared-memory
+                               ring of 3 x 48 KB (1 CTA per SM), 4 x 24 KB
+                               (2 per SM) or 3 x 24 KB (3 per SM); block and
+                               grid are then fixed */
     int pdl;            /* 1 = programmatic dependent launch between passes */
 } bsg_tune;
 

@@ -269,7 +269,7 @@ int enqueue_map_runs(bsg_ctx* c, const bsg::SoA& a, int64_t n, int runs, int mod
 // The bulk-staged kernel reports an expired wait in an error word; any call
 // that synchronises checks it.
 int check_bulk_error(bsg_ctx* c) {
-    if (c->tune.load_path == 3 && bsg::bulk_error_take())
+    if (c->tune.load_path >= 3 && bsg::bulk_error_take())
         return fail(c, BSG_ERR_TIMEOUT, "a bulk-copy wait of the staged map kernel expired");
     return BSG_OK;
 }
@@ -760,7 +760,7 @@ static bool tune_valid(const bsg_tune* t) {
                         (t->vec_per_thread == 4 && t->load_path != 2);
     const bool blk_ok = t->block == 128 || t->block == 256 || t->block == 512;
     return vpt_ok && blk_ok && t->blocks_per_sm >= 0 && t->blocks_per_sm <= 64 &&
-           t->load_path >= 0 && t->load_path <= 3 && (t->pdl == 0 || t->pdl == 1);
+           t->load_path >= 0 && t->load_path <= 5 && (t->pdl == 0 || t->pdl == 1);
 }
 
 int bsg_set_tune(bsg_ctx* c, const bsg_tune* t) {
@@ -870,11 +870,12 @@ extern "C" int bsg_autotune(bsg_ctx* c, size_t n, bsg_tune* out) {
                         best = t;
                     }
                 }
-    // the TMA bulk-staged kernel: one shape (one CTA per SM), with and without PDL
+    // the TMA bulk-staged kernels: three ring shapes, with and without PDL
+    for (int lp : {3, 4, 5})
     for (int pdl : {0, 1}) {
         if (e != cudaSuccess) break;
-        const bsg_tune t{1, 256, 0, 3, pdl};
-        const bsg::MapCfg cfg{1, 256, 0, 3, pdl};
+        const bsg_tune t{1, 256, 0, lp, pdl};
+        const bsg::MapCfg cfg{1, 256, 0, lp, pdl};
         e = bsg::launch_map(a, (int64_t)n, bsg::MODE_FAST, cfg, c->sm_count, c->stream);
         if (e != cudaSuccess) break;
         cudaEventRecord(e0, c->stream);

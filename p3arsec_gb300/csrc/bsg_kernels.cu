@@ -155,24 +155,30 @@ __global__ void __launch_bounds__(256) map_scalar_kernel(SoA a, int64_t n) {
 }
 
 // ------------------------------------------------- TMA bulk-staged variant
-// Each persistent CTA streams whole tiles of kBulkTile options through a
-// kBulkStages-deep ring in shared memory: one thread issues six 1D bulk
-// copies (cp.async.bulk, one per input array) per tile, completing on the
-// stage's mbarrier with a transaction count; every thread waits on the
-// barrier, prices 8 options from shared memory and stores them with 256-bit
-// streaming stores.  The stage is refilled after a block barrier and a proxy
-// fence.  Waits are bounded: on expiry the CTA records kErrBulkTimeout in
-// *err, waits (bounded) for its copies in flight and returns.
+// Each persistent CTA streams whole tiles (256 threads x OPT options) through
+// a STAGES-deep ring in shared memory: one thread issues six 1D bulk copies
+// (cp.async.bulk, one per input array) per tile, completing on the stage's
+// mbarrier with a transaction count; every thread waits on the barrier,
+// prices OPT options from shared memory and stores them with streaming
+// stores.  A stage is refilled after a block barrier and a proxy fence.
+// Waits are bounded: on expiry the CTA records kErrBulkTimeout in
+// g_bulk_err, waits (bounded) for its copies in flight and returns.
+// Shapes: <8, 3> 144 KB per CTA (1 per SM), <4, 4> 96 KB (2 per SM),
+// <4, 3> 72 KB (3 per SM).
 constexpr int kBulkThreads = 256;
-constexpr int kBulkTile = kBulkThreads * 8;          // 2048 options per tile
-constexpr int kBulkStages = 3;
-constexpr int kBulkStageBytes = 6 * kBulkTile * 4;   // 48 KB
 constexpr unsigned kErrBulkTimeout = 1u;
 constexpr uint32_t kBulkWaitLimit = 1u << 22;
 
-// Error word of the bulk kernel (kErrBulkTimeout); read and cleared by the
+// Error word of the bulk kernels (kErrBulkTimeout); read and cleared by the
 // host with bulk_error_take().
 __device__ unsigned g_bulk_err;
+
+template <int OPT, int STAGES>
+struct BulkShape {
+    static constexpr int tile = kBulkThreads * OPT;
+    static constexpr int stage_bytes = 6 * tile * 4;
+    static constexpr int smem = STAGES * stage_bytes;
+};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -194,102 +200,103 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity)
     return false;
 }
 
-// One 1D bulk copy of a tile's worth of one array (kBulkTile * 4 bytes,
-// 16-byte aligned at both ends) into shared memory, completing on `bar`.
-__device__ __forceinline__ void bulk_copy(char* dst, const char* src, uint32_t bar) {
+// One 1D bulk copy of `bytes` (16-byte aligned at both ends, a multiple of
+// 16) into shared memory, completing on `bar`.
+__device__ __forceinline__ void bulk_copy(char* dst, const char* src, int bytes, uint32_t bar) {
     asm volatile(
         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-        :: "r"(smem_u32(dst)), "l"(src), "r"(kBulkTile * 4), "r"(bar) : "memory");
+        :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(bar) : "memory");
 }
 
 // Issues the six copies of tile `tile` into stage memory `st` (thread 0).
+template <int TILE>
 __device__ __forceinline__ void bulk_issue(const SoA& a, int64_t tile, char* st, uint32_t bar) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-                 :: "r"(bar), "r"(kBulkStageBytes) : "memory");
-    const size_t off = (size_t)tile * kBulkTile * 4;
-    bulk_copy(st + 0 * kBulkTile * 4, reinterpret_cast<const char*>(a.s) + off, bar);
-    bulk_copy(st + 1 * kBulkTile * 4, reinterpret_cast<const char*>(a.k) + off, bar);
-    bulk_copy(st + 2 * kBulkTile * 4, reinterpret_cast<const char*>(a.r) + off, bar);
-    bulk_copy(st + 3 * kBulkTile * 4, reinterpret_cast<const char*>(a.v) + off, bar);
-    bulk_copy(st + 4 * kBulkTile * 4, reinterpret_cast<const char*>(a.t) + off, bar);
-    bulk_copy(st + 5 * kBulkTile * 4, reinterpret_cast<const char*>(a.ot) + off, bar);
+                 :: "r"(bar), "r"(6 * TILE * 4) : "memory");
+    const size_t off = (size_t)tile * TILE * 4;
+    bulk_copy(st + 0 * TILE * 4, reinterpret_cast<const char*>(a.s) + off, TILE * 4, bar);
+    bulk_copy(st + 1 * TILE * 4, reinterpret_cast<const char*>(a.k) + off, TILE * 4, bar);
+    bulk_copy(st + 2 * TILE * 4, reinterpret_cast<const char*>(a.r) + off, TILE * 4, bar);
+    bulk_copy(st + 3 * TILE * 4, reinterpret_cast<const char*>(a.v) + off, TILE * 4, bar);
+    bulk_copy(st + 4 * TILE * 4, reinterpret_cast<const char*>(a.t) + off, TILE * 4, bar);
+    bulk_copy(st + 5 * TILE * 4, reinterpret_cast<const char*>(a.ot) + off, TILE * 4, bar);
 }
 
-template <int M>
+template <int M, int OPT, int STAGES>
 __global__ void __launch_bounds__(kBulkThreads) map_bulk_kernel(SoA a, int64_t n) {
+    using B = BulkShape<OPT, STAGES>;
+    constexpr int TILE = B::tile;
     extern __shared__ __align__(128) char smem[];
-    __shared__ __align__(8) unsigned long long bars[kBulkStages];
+    __shared__ __align__(8) unsigned long long bars[STAGES];
     __shared__ int sh_abort;
     pdl_trigger();
-    const int64_t ntiles = n / kBulkTile;
+    const int64_t ntiles = n / TILE;
     // tiles of this CTA: blockIdx.x + k * gridDim.x
     const int64_t mine = (ntiles > blockIdx.x) ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kBulkStages; ++s)
+        for (int s = 0; s < STAGES; ++s)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(smem_u32(&bars[s])) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         sh_abort = 0;
-        for (int s = 0; s < kBulkStages && s < mine; ++s)
-            bulk_issue(a, blockIdx.x + (int64_t)s * gridDim.x, smem + s * kBulkStageBytes,
-                       smem_u32(&bars[s]));
+        for (int s = 0; s < STAGES && s < mine; ++s)
+            bulk_issue<TILE>(a, blockIdx.x + (int64_t)s * gridDim.x, smem + s * B::stage_bytes,
+                             smem_u32(&bars[s]));
     }
     __syncthreads();
     int64_t k = 0;
     for (; k < mine; ++k) {
-        const int s = (int)(k % kBulkStages);
-        const uint32_t parity = (uint32_t)((k / kBulkStages) & 1);
+        const int s = (int)(k % STAGES);
+        const uint32_t parity = (uint32_t)((k / STAGES) & 1);
         const bool ok = mbar_wait_bounded(smem_u32(&bars[s]), parity);
         if (!ok) sh_abort = 1;  // benign race: every writer stores 1
         __syncthreads();
         if (sh_abort) break;
-        const char* st = smem + s * kBulkStageBytes;
+        const char* st = smem + s * B::stage_bytes;
         const int64_t tile = blockIdx.x + k * gridDim.x;
-        // thread t prices options 4t..4t+3 and 1024+4t..1024+4t+3 of the
-        // tile, so each 128-bit shared load and global store of a warp
-        // covers 512 contiguous bytes (no bank conflicts)
-        float p[2][4];
+        // thread t prices options 4t..4t+3 of each 1024-option slice, so each
+        // 128-bit shared load and global store of a warp covers 512
+        // contiguous bytes (no bank conflicts)
+        float p[OPT / 4][4];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
+        for (int h = 0; h < OPT / 4; ++h) {
             const int o = (4 * threadIdx.x + 1024 * h) * 4;
-            const float4 S = *reinterpret_cast<const float4*>(st + 0 * kBulkTile * 4 + o);
-            const float4 K = *reinterpret_cast<const float4*>(st + 1 * kBulkTile * 4 + o);
-            const float4 R = *reinterpret_cast<const float4*>(st + 2 * kBulkTile * 4 + o);
-            const float4 V = *reinterpret_cast<const float4*>(st + 3 * kBulkTile * 4 + o);
-            const float4 T = *reinterpret_cast<const float4*>(st + 4 * kBulkTile * 4 + o);
-            const int4 O = *reinterpret_cast<const int4*>(st + 5 * kBulkTile * 4 + o);
+            const float4 S = *reinterpret_cast<const float4*>(st + 0 * TILE * 4 + o);
+            const float4 K = *reinterpret_cast<const float4*>(st + 1 * TILE * 4 + o);
+            const float4 R = *reinterpret_cast<const float4*>(st + 2 * TILE * 4 + o);
+            const float4 V = *reinterpret_cast<const float4*>(st + 3 * TILE * 4 + o);
+            const float4 T = *reinterpret_cast<const float4*>(st + 4 * TILE * 4 + o);
+            const int4 O = *reinterpret_cast<const int4*>(st + 5 * TILE * 4 + o);
             p[h][0] = price<M>(S.x, K.x, R.x, V.x, T.x, O.x);
             p[h][1] = price<M>(S.y, K.y, R.y, V.y, T.y, O.y);
             p[h][2] = price<M>(S.z, K.z, R.z, V.z, T.z, O.z);
             p[h][3] = price<M>(S.w, K.w, R.w, V.w, T.w, O.w);
         }
         __syncthreads();  // every thread has read stage s
-        if (threadIdx.x == 0 && k + kBulkStages < mine) {
+        if (threadIdx.x == 0 && k + STAGES < mine) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            bulk_issue(a, blockIdx.x + (k + kBulkStages) * gridDim.x,
-                       smem + s * kBulkStageBytes, smem_u32(&bars[s]));
+            bulk_issue<TILE>(a, blockIdx.x + (k + STAGES) * gridDim.x, smem + s * B::stage_bytes,
+                             smem_u32(&bars[s]));
         }
-        st_group<4>(a.out + tile * kBulkTile + 4 * threadIdx.x, p[0]);
-        st_group<4>(a.out + tile * kBulkTile + 1024 + 4 * threadIdx.x, p[1]);
+#pragma unroll
+        for (int h = 0; h < OPT / 4; ++h)
+            st_group<4>(a.out + tile * TILE + 1024 * h + 4 * threadIdx.x, p[h]);
     }
     if (k < mine) {
         // timed out: record it, let this CTA's copies in flight land (bounded)
         if (threadIdx.x == 0) {
             atomicOr(&g_bulk_err, kErrBulkTimeout);
-            for (int64_t q = k; q < mine && q < k + kBulkStages; ++q)
-                mbar_wait_bounded(smem_u32(&bars[q % kBulkStages]),
-                                  (uint32_t)((q / kBulkStages) & 1));
+            for (int64_t q = k; q < mine && q < k + STAGES; ++q)
+                mbar_wait_bounded(smem_u32(&bars[q % STAGES]), (uint32_t)((q / STAGES) & 1));
         }
         __syncthreads();
         return;
     }
     // options past the last whole tile: the last CTA, one per thread
     if (blockIdx.x == gridDim.x - 1)
-        for (int64_t i = ntiles * kBulkTile + threadIdx.x; i < n; i += kBulkThreads)
+        for (int64_t i = ntiles * TILE + threadIdx.x; i < n; i += kBulkThreads)
             price_scalar<M>(a, i);
     pdl_wait();
 }
-
-size_t bulk_smem_bytes() { return (size_t)kBulkStages * kBulkStageBytes; }
 
 unsigned bulk_error_take() {
     unsigned v = 0, zero = 0;
@@ -312,35 +319,36 @@ bool map_vectorizable(const SoA& a, const MapCfg& cfg) {
            aligned(a.out, al);
 }
 
-template <int M>
+template <int M, int OPT, int STAGES>
 static cudaError_t launch_map_bulk(const SoA& a, int64_t n, const MapCfg& cfg, int sm_count,
                                   cudaStream_t st) {
-    // opt in to the 144 KB of dynamic shared memory, once per device
+    using B = BulkShape<OPT, STAGES>;
+    // opt in to the dynamic shared memory, once per device
     static unsigned long long opted = 0;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 64 && !(opted & (1ull << dev))) {
-        e = cudaFuncSetAttribute(map_bulk_kernel<M>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)bulk_smem_bytes());
+        e = cudaFuncSetAttribute(map_bulk_kernel<M, OPT, STAGES>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, B::smem);
         if (e != cudaSuccess) return e;
         opted |= 1ull << dev;
     }
-    const int64_t ntiles = n / kBulkTile;
-    int64_t grid = (int64_t)sm_count;  // one CTA per SM (144 KB of staging each)
+    const int64_t ntiles = n / B::tile;
+    int64_t grid = (int64_t)sm_count * (220 * 1024 / B::smem);  // CTAs that fit per SM
     if (grid > ntiles) grid = ntiles;
     if (grid < 1) grid = 1;
     cudaLaunchConfig_t lc = {};
     lc.gridDim = dim3((unsigned)grid);
     lc.blockDim = dim3(kBulkThreads);
-    lc.dynamicSmemBytes = bulk_smem_bytes();
+    lc.dynamicSmemBytes = B::smem;
     lc.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     lc.attrs = attr;
     lc.numAttrs = cfg.pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&lc, map_bulk_kernel<M>, a, n);
+    return cudaLaunchKernelEx(&lc, map_bulk_kernel<M, OPT, STAGES>, a, n);
 }
 
 template <int M>
@@ -355,9 +363,16 @@ static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg,
         map_scalar_kernel<M><<<(unsigned)grid, 256, 0, st>>>(a, n);
         return cudaGetLastError();
     }
-    if (cfg.load_path == 3) {
-        if constexpr (M == MODE_FAST)
-            if (n >= kBulkTile) return launch_map_bulk<M>(a, n, cfg, sm_count, st);
+    if (cfg.load_path >= 3) {
+        if constexpr (M == MODE_FAST) {
+            // 3: <8 options, 3 stages>, 4: <4, 4>, 5: <4, 3>
+            if (cfg.load_path == 3 && n >= BulkShape<8, 3>::tile)
+                return launch_map_bulk<M, 8, 3>(a, n, cfg, sm_count, st);
+            if (cfg.load_path == 4 && n >= BulkShape<4, 4>::tile)
+                return launch_map_bulk<M, 4, 4>(a, n, cfg, sm_count, st);
+            if (cfg.load_path == 5 && n >= BulkShape<4, 3>::tile)
+                return launch_map_bulk<M, 4, 3>(a, n, cfg, sm_count, st);
+        }
         MapCfg v8 = cfg;  // too small for a whole tile (or another mode): 256-bit loads
         v8.load_path = 2;
         v8.vpt = 1;

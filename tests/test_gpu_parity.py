@@ -125,7 +125,7 @@ def test_all_tunings_give_identical_bits(gpu_ctx):
     base = gpu_ctx.price_book(book)
     saved = gpu_ctx.get_tune()
     try:
-        for lp in (0, 1, 2, 3):
+        for lp in (0, 1, 2, 3, 4, 5):
             for vpt in (1, 2, 4):
                 if lp >= 2 and vpt == 4:
                     continue
@@ -213,9 +213,10 @@ def test_bulk_staged_path_bits_and_tails(gpu_ctx, n):
     base = gpu_ctx.price_book(book)
     saved = gpu_ctx.get_tune()
     try:
-        for pdl in (0, 1):
-            gpu_ctx.set_tune(1, 256, 0, 3, pdl)
-            got = gpu_ctx.price_book(book, num_runs=5)
-            assert np.array_equal(got.view(np.uint32), base.view(np.uint32))
+        for lp in (3, 4, 5):
+            for pdl in (0, 1):
+                gpu_ctx.set_tune(1, 256, 0, lp, pdl)
+                got = gpu_ctx.price_book(book, num_runs=5)
+                assert np.array_equal(got.view(np.uint32), base.view(np.uint32)), (lp, pdl)
     finally:
         gpu_ctx.set_tune(**saved)
