@@ -34,11 +34,12 @@ BYTES_PER_OPTION = 28  # 5 float inputs + int32 otype + float price
 METRIC = "options/sec & %HBM roofline"
 UNIT = "options/s"
 SEED = 20241203
-# DRAM bytes per option per pass of the fast map kernel, from the ncu capture
-# summarised in profiles/map_fast_10M.md (dram__bytes_read.sum +
-# dram__bytes_write.sum of one 10M-option launch / 10M); traffic grows in
-# proportion to the options of a launch.
-NCU_DRAM_BYTES_PER_OPTION = 26.79
+# Steady-state DRAM bytes per option per pass of the fast map kernel by load
+# path, from warm ncu captures (dram__bytes_read.sum + dram__bytes_write.sum
+# of mid-run 10M-option launches / 10M) summarised in
+# profiles/map_fast_10M.md; traffic grows in proportion to the options of a
+# launch.  Shapes not captured report null.
+NCU_DRAM_BYTES_PER_OPTION = {1: 20.60, 2: 26.61}
 NCU_PROFILE = "profiles/map_fast_10M.md"
 
 
@@ -249,9 +250,10 @@ def run_ours(args, rank, world, local):
                    "tune": tune, "mode": "fast"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src,
-                     "traffic": (NCU_DRAM_BYTES_PER_OPTION * n
-                                 if NCU_DRAM_BYTES_PER_OPTION else None),
-                     "traffic_source": NCU_PROFILE if NCU_DRAM_BYTES_PER_OPTION else None,
+                     "traffic": (NCU_DRAM_BYTES_PER_OPTION[tune["load_path"]] * n
+                                 if tune["load_path"] in NCU_DRAM_BYTES_PER_OPTION else None),
+                     "traffic_source": (NCU_PROFILE + " (warm, steady state)"
+                                        if tune["load_path"] in NCU_DRAM_BYTES_PER_OPTION else None),
                      "bytes_per_launch": BYTES_PER_OPTION * n,
                      "avg_launch_us": per_launch_s * 1e6},
         "accuracy": accuracy,
