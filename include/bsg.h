@@ -347,6 +347,14 @@ typedef struct bsg_tune {
 } bsg_tune;
 
 int bsg_autotune(bsg_ctx* ctx, size_t n, bsg_tune* out);
+
+/* Self-test of the device-side failure detection: launches the staged map
+ * kernel with every mbarrier expecting more bytes than its copies deliver,
+ * so each of its waits runs out after limit_s (0 < limit_s <= 10) of GPU
+ * time; the kernel records the expiry, lets its copies land and returns.
+ * Expected result: BSG_ERR_TIMEOUT, the context still usable afterwards.
+ * elapsed_s (optional): host time of the call. */
+int bsg_selftest_wait_timeout(bsg_ctx* ctx, double limit_s, double* elapsed_s);
 int bsg_get_tune(const bsg_ctx* ctx, bsg_tune* out);
 int bsg_set_tune(bsg_ctx* ctx, const bsg_tune* tune);
 

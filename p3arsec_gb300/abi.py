@@ -160,6 +160,7 @@ SIGNATURES = {
     "bsg_write_soa": (_I, [ctypes.c_char_p, ctypes.POINTER(BookC)]),
     "bsg_read_soa": (_I, [ctypes.c_char_p, ctypes.POINTER(BookC)]),
     "bsg_autotune": (_I, [_P, _SZ, ctypes.POINTER(Tune)]),
+    "bsg_selftest_wait_timeout": (_I, [_P, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
     "bsg_get_tune": (_I, [_P, ctypes.POINTER(Tune)]),
     "bsg_set_tune": (_I, [_P, ctypes.POINTER(Tune)]),
 }
@@ -333,6 +334,12 @@ class Context:
         st = self.lib.bsg_autotune(self.h, n, ctypes.byref(t))
         _check(self.lib, self.h, st)
         return t.as_dict()
+
+    def selftest_wait_timeout(self, limit_s: float = 0.05):
+        """Makes the staged kernel's bounded waits expire; returns (status, seconds)."""
+        el = ctypes.c_double()
+        st = self.lib.bsg_selftest_wait_timeout(self.h, limit_s, ctypes.byref(el))
+        return st, el.value
 
     def get_tune(self) -> dict:
         t = Tune()

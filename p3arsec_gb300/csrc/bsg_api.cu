@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -742,6 +743,29 @@ int bsg_error_report(bsg_ctx* c, const float* s, const float* k, const float* r,
         std::memcpy(&b, &h[i].max_price_bits, 8); std::memcpy(&out[i].max_price, &b, 8);
         out[i].sum_sq_abs = h[i].sum_sq;
     }
+    return BSG_OK;
+}
+
+int bsg_selftest_wait_timeout(bsg_ctx* c, double limit_s, double* elapsed_s) {
+    if (!c || !(limit_s > 0) || limit_s > 10.0) return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mu);
+    BSG_CK(c, cudaSetDevice(c->device));
+    const size_t n = 4096;  // one tile of the <4, 4> ring per CTA that runs
+    if (n > c->cap) return fail(c, BSG_ERR_CAPACITY, "context too small for the self-test");
+    bsg::bulk_error_take();
+    const bsg::SoA d = c->resident(n);
+    cudaError_t e = bsg::launch_fill(d, (int64_t)n, 7u, c->sm_count, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "launch_fill");
+    const auto t0 = std::chrono::steady_clock::now();
+    e = bsg::launch_bulk_wait_selftest(d, (int64_t)n, c->sm_count, (uint64_t)(limit_s * 1e9),
+                                       c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "launch_bulk_wait_selftest");
+    c->launches += 2;
+    BSG_CK(c, cudaStreamSynchronize(c->stream));
+    if (elapsed_s)
+        *elapsed_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (bsg::bulk_error_take())
+        return fail(c, BSG_ERR_TIMEOUT, "the staged kernel's bounded wait expired (self-test)");
     return BSG_OK;
 }
 

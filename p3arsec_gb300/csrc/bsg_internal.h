@@ -61,6 +61,11 @@ cudaError_t launch_map(const SoA& a, int64_t n, int mode, const MapCfg& cfg,
 // Reads and clears the bulk-staged kernel's error word (non-zero: a bounded
 // wait expired and some tiles were not priced).
 unsigned bulk_error_take();
+// Launches the bulk-staged kernel with every barrier expecting 16 bytes more
+// than its copies deliver, so each wait expires after wait_ns (self-test of
+// the bounded waits; the copies themselves complete normally).
+cudaError_t launch_bulk_wait_selftest(const SoA& a, int64_t n, int sm_count, uint64_t wait_ns,
+                                      cudaStream_t st);
 // True when launch_map would take the vector path for these pointers.
 bool map_vectorizable(const SoA& a, const MapCfg& cfg);
 

@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(256) map_scalar_kernel(SoA a, int64_t n) {
 // <4, 3> 72 KB (3 per SM).
 constexpr int kBulkThreads = 256;
 constexpr unsigned kErrBulkTimeout = 1u;
-constexpr uint32_t kBulkWaitLimit = 1u << 22;
+constexpr uint64_t kBulkWaitNs = 1000000000ull;  // bound of one wait: 1 s
 
 // Error word of the bulk kernels (kErrBulkTimeout); read and cleared by the
 // host with bulk_error_take().
@@ -194,10 +194,21 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     return ok != 0;
 }
 
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
-    for (uint32_t i = 0; i < kBulkWaitLimit; ++i)
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits for the phase of `bar` with parity `parity` for at most limit_ns of
+// wall time (the GPU's global timer); false when the bound expired.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, uint64_t limit_ns) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (;;) {
         if (mbar_try_wait(bar, parity)) return true;
-    return false;
+        if (global_ns() - t0 > limit_ns) return false;
+    }
 }
 
 // One 1D bulk copy of `bytes` (16-byte aligned at both ends, a multiple of
@@ -209,10 +220,14 @@ __device__ __forceinline__ void bulk_copy(char* dst, const char* src, int bytes,
 }
 
 // Issues the six copies of tile `tile` into stage memory `st` (thread 0).
+// tx_extra (0 in production) raises the barrier's expected byte count above
+// what the copies deliver, so that its phase can never complete: the
+// self-test of the bounded waits.
 template <int TILE>
-__device__ __forceinline__ void bulk_issue(const SoA& a, int64_t tile, char* st, uint32_t bar) {
+__device__ __forceinline__ void bulk_issue(const SoA& a, int64_t tile, char* st, uint32_t bar,
+                                           uint32_t tx_extra) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-                 :: "r"(bar), "r"(6 * TILE * 4) : "memory");
+                 :: "r"(bar), "r"(6 * TILE * 4 + tx_extra) : "memory");
     const size_t off = (size_t)tile * TILE * 4;
     bulk_copy(st + 0 * TILE * 4, reinterpret_cast<const char*>(a.s) + off, TILE * 4, bar);
     bulk_copy(st + 1 * TILE * 4, reinterpret_cast<const char*>(a.k) + off, TILE * 4, bar);
@@ -223,7 +238,8 @@ __device__ __forceinline__ void bulk_issue(const SoA& a, int64_t tile, char* st,
 }
 
 template <int M, int OPT, int STAGES>
-__global__ void __launch_bounds__(kBulkThreads) map_bulk_kernel(SoA a, int64_t n) {
+__global__ void __launch_bounds__(kBulkThreads) map_bulk_kernel(SoA a, int64_t n, uint64_t wait_ns,
+                                                                 uint32_t tx_extra) {
     using B = BulkShape<OPT, STAGES>;
     constexpr int TILE = B::tile;
     extern __shared__ __align__(128) char smem[];
@@ -240,14 +256,14 @@ __global__ void __launch_bounds__(kBulkThreads) map_bulk_kernel(SoA a, int64_t n
         sh_abort = 0;
         for (int s = 0; s < STAGES && s < mine; ++s)
             bulk_issue<TILE>(a, blockIdx.x + (int64_t)s * gridDim.x, smem + s * B::stage_bytes,
-                             smem_u32(&bars[s]));
+                             smem_u32(&bars[s]), tx_extra);
     }
     __syncthreads();
     int64_t k = 0;
     for (; k < mine; ++k) {
         const int s = (int)(k % STAGES);
         const uint32_t parity = (uint32_t)((k / STAGES) & 1);
-        const bool ok = mbar_wait_bounded(smem_u32(&bars[s]), parity);
+        const bool ok = mbar_wait_bounded(smem_u32(&bars[s]), parity, wait_ns);
         if (!ok) sh_abort = 1;  // benign race: every writer stores 1
         __syncthreads();
         if (sh_abort) break;
@@ -275,7 +291,7 @@ __global__ void __launch_bounds__(kBulkThreads) map_bulk_kernel(SoA a, int64_t n
         if (threadIdx.x == 0 && k + STAGES < mine) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             bulk_issue<TILE>(a, blockIdx.x + (k + STAGES) * gridDim.x, smem + s * B::stage_bytes,
-                             smem_u32(&bars[s]));
+                             smem_u32(&bars[s]), tx_extra);
         }
 #pragma unroll
         for (int h = 0; h < OPT / 4; ++h)
@@ -286,7 +302,7 @@ __global__ void __launch_bounds__(kBulkThreads) map_bulk_kernel(SoA a, int64_t n
         if (threadIdx.x == 0) {
             atomicOr(&g_bulk_err, kErrBulkTimeout);
             for (int64_t q = k; q < mine && q < k + STAGES; ++q)
-                mbar_wait_bounded(smem_u32(&bars[q % STAGES]), (uint32_t)((q / STAGES) & 1));
+                mbar_wait_bounded(smem_u32(&bars[q % STAGES]), (uint32_t)((q / STAGES) & 1), wait_ns);
         }
         __syncthreads();
         return;
@@ -321,7 +337,8 @@ bool map_vectorizable(const SoA& a, const MapCfg& cfg) {
 
 template <int M, int OPT, int STAGES>
 static cudaError_t launch_map_bulk(const SoA& a, int64_t n, const MapCfg& cfg, int sm_count,
-                                  cudaStream_t st) {
+                                  cudaStream_t st, uint64_t wait_ns = kBulkWaitNs,
+                                  uint32_t tx_extra = 0) {
     using B = BulkShape<OPT, STAGES>;
     // opt in to the dynamic shared memory, once per device
     static unsigned long long opted = 0;
@@ -348,7 +365,7 @@ static cudaError_t launch_map_bulk(const SoA& a, int64_t n, const MapCfg& cfg, i
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     lc.attrs = attr;
     lc.numAttrs = cfg.pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&lc, map_bulk_kernel<M, OPT, STAGES>, a, n);
+    return cudaLaunchKernelEx(&lc, map_bulk_kernel<M, OPT, STAGES>, a, n, wait_ns, tx_extra);
 }
 
 template <int M>
@@ -423,6 +440,13 @@ static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg,
 #undef BSG_LAUNCH
     if (le != cudaSuccess) return le;
     return cudaGetLastError();
+}
+
+cudaError_t launch_bulk_wait_selftest(const SoA& a, int64_t n, int sm_count, uint64_t wait_ns,
+                                      cudaStream_t st) {
+    if (n < BulkShape<4, 4>::tile) return cudaErrorInvalidValue;
+    const MapCfg cfg{1, kBulkThreads, 0, 4, 0};
+    return launch_map_bulk<MODE_FAST, 4, 4>(a, n, cfg, sm_count, st, wait_ns, 16u);
 }
 
 cudaError_t launch_map(const SoA& a, int64_t n, int mode, const MapCfg& cfg,
