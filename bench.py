@@ -455,8 +455,10 @@ def run_serve(args, rank, world, local):
         for rate in rates:
             res = abi.serve_trace(host, out, rate_per_s=rate, duration_s=args.serve_seconds,
                                   min_n=16, max_n=1 << 20, seed=SEED + int(rate),
-                                  device=local, budget_bytes=64 << 30, max_inflight=4,
-                                  plain=(mode == "plain"), drain_timeout_s=60.0)
+                                  device=local, budget_bytes=64 << 30,
+                                  max_inflight=args.serve_inflight,
+                                  plain=(mode == "plain"), drain_timeout_s=60.0,
+                                  fused=(mode == "batched" and args.serve_fused))
             res["rate_per_s"] = rate
             sweep[mode].append(res)
             print(json.dumps({"serve_point": mode, **res}), file=sys.stderr, flush=True)
@@ -486,7 +488,8 @@ def run_serve(args, rank, world, local):
         "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded trace and books)",
         "config": {"workload": f"open-loop Poisson trace at {args.serve_rate:g} req/s for "
                                f"{args.serve_seconds:g} s, sizes log-uniform in [16, 2^20], "
-                               "64 GB device budget, 4 batches in flight",
+                               f"64 GB device budget, {args.serve_inflight} batches in flight",
+                   "fused": bool(args.serve_fused),
                    "rates_swept": rates, "seconds_per_point": args.serve_seconds},
         "latency_s": {"p50": a["p50_s"], "p99": a["p99_s"], "p999": a["p999_s"], "max": a["max_s"]},
         "plain_at_rate": {k: at["plain"][k] for k in ("options_per_s", "p50_s", "p99_s", "p999_s",
@@ -674,8 +677,11 @@ def main(argv=None):
                     default="map")
     ap.add_argument("--serve-rate", type=float, default=20000.0)
     ap.add_argument("--serve-rates",
-                    default="1000,5000,10000,15000,20000,30000,40000,50000,60000,70000,80000")
+                    default="1000,5000,10000,15000,20000,30000,40000,50000,60000,70000,80000,90000")
     ap.add_argument("--serve-seconds", type=float, default=3.0)
+    ap.add_argument("--serve-inflight", type=int, default=4)
+    ap.add_argument("--serve-fused", type=int, default=1,
+                    help="1: one fused kernel per batch; 0: gather, price, scatter")
     ap.add_argument("--books", type=int, default=4096, help="batch config: number of books")
     ap.add_argument("--n", type=int, default=N_OPTIONS)
     ap.add_argument("--runs", type=int, default=NUM_RUNS)

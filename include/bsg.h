@@ -199,7 +199,8 @@ int bsg_error_report(bsg_ctx* ctx, const float* sptprice, const float* strike,
  * kernel gathers their inputs from pinned host memory into the pool, the
  * persistent batch kernel prices them, one kernel writes the prices back to
  * each request's host output.  Up to max_inflight batches overlap on the
- * GPU (one stream each).  With plain = 1 the loop instead prices one request
+ * GPU (one stream each).  With fused = 1 the three steps are one kernel.
+ * With plain = 1 the loop instead prices one request
  * at a time with per-array copies and one plain map launch (the baseline).
  * Request arrays are host memory; pinned memory (bsg_host_alloc or
  * cudaHostRegister) is required for the batched path and recommended for the
@@ -215,6 +216,10 @@ typedef struct bsg_server_config {
     int plain;                /* 1 = one plain launch per request, serially */
     unsigned flags;           /* BSG_MODE_* */
     double batch_timeout_s;   /* bound on waiting for one batch (0 = 30 s) */
+    int fused;                /* 1 = one kernel per batch reads the inputs from
+                                 host memory, prices them and writes the prices
+                                 back (the pool then only accounts the budget);
+                                 0 = gather into the pool, price, scatter */
 } bsg_server_config;
 
 typedef struct bsg_request {

@@ -19,6 +19,7 @@
 // six host-to-device copies, one plain map launch, one device-to-host copy.
 #include "bsg.h"
 #include "bsg_internal.h"
+#include "bsg_math.cuh"
 
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -131,6 +132,75 @@ __global__ void __launch_bounds__(kThreads) egress_kernel(const Desc* __restrict
     }
 }
 
+// Fused path: one kernel per batch reads each request's inputs from host
+// memory, prices them and writes the prices back to the request's host
+// output.  Tiles come from a per-slot counter that only grows: this launch's
+// tiles are [base, base + ntiles) of it, and every block ends with exactly
+// one failing increment, so the next launch's base is base + ntiles + grid
+// (no reset between batches).
+template <int M>
+__global__ void __launch_bounds__(kThreads) serve_fused_kernel(const Desc* __restrict__ d,
+                                                               const uint64_t* __restrict__ pre,
+                                                               int m, uint64_t ntiles,
+                                                               unsigned long long* counter,
+                                                               unsigned long long base) {
+    __shared__ int sh_q, sh_done;
+    __shared__ uint64_t sh_tile;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const unsigned long long t = atomicAdd(counter, 1ull) - base;
+            sh_done = t >= ntiles;
+            if (!sh_done) {
+                sh_tile = t;
+                sh_q = find_segment(pre, m, t);
+            }
+        }
+        __syncthreads();
+        if (sh_done) break;
+        const int qi = sh_q;
+        const uint64_t tile = sh_tile;
+        __syncthreads();
+        const Desc q = d[qi];
+        const uint64_t b = (tile - pre[qi]) * kTile;
+        const uint64_t e = (b + kTile < q.n) ? b + kTile : q.n;
+        const uint64_t e4 = q.vec ? b + ((e - b) & ~3ull) : b;
+        for (uint64_t g = b / 4 + threadIdx.x; g < e4 / 4; g += kThreads) {
+            const float4 S = reinterpret_cast<const float4*>(q.src[0])[g];
+            const float4 K = reinterpret_cast<const float4*>(q.src[1])[g];
+            const float4 R = reinterpret_cast<const float4*>(q.src[2])[g];
+            const float4 V = reinterpret_cast<const float4*>(q.src[3])[g];
+            const float4 T = reinterpret_cast<const float4*>(q.src[4])[g];
+            const int4 O = reinterpret_cast<const int4*>(q.ot)[g];
+            float4 P;
+            P.x = bsg::price<M>(S.x, K.x, R.x, V.x, T.x, O.x);
+            P.y = bsg::price<M>(S.y, K.y, R.y, V.y, T.y, O.y);
+            P.z = bsg::price<M>(S.z, K.z, R.z, V.z, T.z, O.z);
+            P.w = bsg::price<M>(S.w, K.w, R.w, V.w, T.w, O.w);
+            reinterpret_cast<float4*>(q.out)[g] = P;
+        }
+        for (uint64_t i = e4 + threadIdx.x; i < e; i += kThreads)
+            q.out[i] = bsg::price<M>(q.src[0][i], q.src[1][i], q.src[2][i], q.src[3][i],
+                                     q.src[4][i], q.ot[i]);
+    }
+}
+
+cudaError_t launch_fused(int mode, unsigned grid, cudaStream_t st, const Desc* d,
+                         const uint64_t* pre, int m, uint64_t ntiles,
+                         unsigned long long* counter, unsigned long long base) {
+    switch (mode) {
+        case bsg::MODE_FAST:
+            serve_fused_kernel<bsg::MODE_FAST><<<grid, kThreads, 0, st>>>(d, pre, m, ntiles, counter, base);
+            break;
+        case bsg::MODE_SFU_REF:
+            serve_fused_kernel<bsg::MODE_SFU_REF><<<grid, kThreads, 0, st>>>(d, pre, m, ntiles, counter, base);
+            break;
+        default:
+            serve_fused_kernel<bsg::MODE_LIBM_REF><<<grid, kThreads, 0, st>>>(d, pre, m, ntiles, counter, base);
+            break;
+    }
+    return cudaGetLastError();
+}
+
 enum State { Q_QUEUED, Q_ADMITTED, Q_DONE };
 
 struct Request {
@@ -153,6 +223,7 @@ struct Slot {
     char* h_tab = nullptr;  // pinned table block
     char* d_tab = nullptr;  // device table block
     unsigned long long* d_cursor = nullptr;
+    unsigned long long fused_base = 0;  // next launch's base on the fused counter
     std::vector<Request*> reqs;
     bool busy = false;
 };
@@ -285,6 +356,15 @@ struct bsg_server {
         const uint64_t* dlen = doff + m;
         const uint64_t* dpre = dlen + m;
         const unsigned grid = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)sm_count * 8);
+        if (cfg.fused) {
+            // counter lives after the batch kernel's cursor word
+            unsigned long long* ctr = sl.d_cursor + 1;
+            if (launch_fused(mode, grid, sl.st, dd, dpre, m, ntiles, ctr, sl.fused_base) != cudaSuccess)
+                return BSG_ERR_CUDA;
+            sl.fused_base += ntiles + grid;
+            if (cudaEventRecord(sl.ev, sl.st) != cudaSuccess) return BSG_ERR_CUDA;
+            return BSG_OK;
+        }
         ingest_kernel<<<grid, kThreads, 0, sl.st>>>(dd, dpre, m, ntiles, pool);
         if (cudaGetLastError() != cudaSuccess) return BSG_ERR_CUDA;
         if (cudaMemsetAsync(sl.d_cursor, 0, sizeof(unsigned long long), sl.st) != cudaSuccess)
@@ -399,7 +479,7 @@ struct bsg_server {
                 cv_done.notify_all();
                 continue;
             }
-            st.kernel_launches += cfg.plain ? 1 : 3;
+            st.kernel_launches += (cfg.plain || cfg.fused) ? 1 : 3;
             inflight.push_back(si);
             cv_comp.notify_one();
         }
@@ -577,7 +657,8 @@ int bsg_server_create(bsg_server** out, const bsg_server_config* cfg) {
                 break;
             }
             if (cudaMallocHost(&sl.h_tab, tb) != cudaSuccess || cudaMalloc(&sl.d_tab, tb) != cudaSuccess ||
-                cudaMalloc(&sl.d_cursor, 256) != cudaSuccess) {
+                cudaMalloc(&sl.d_cursor, 256) != cudaSuccess ||
+                cudaMemset(sl.d_cursor, 0, 256) != cudaSuccess) {
                 rc = BSG_ERR_OUT_OF_MEMORY;
                 break;
             }

@@ -35,7 +35,8 @@ def disjoint_requests(rng, pool_n, count, max_n):
     return reqs
 
 
-def test_each_result_same_alone_and_in_mix(gpu_ctx):
+@pytest.mark.parametrize("fused", [False, True])
+def test_each_result_same_alone_and_in_mix(gpu_ctx, fused):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(5)
     pool_n = 1 << 21
@@ -43,7 +44,7 @@ def test_each_result_same_alone_and_in_mix(gpu_ctx):
     mix = pinned_zeros(torch, pool_n)
     alone = pinned_zeros(torch, pool_n)
     reqs = disjoint_requests(rng, pool_n, 400, 40000)
-    with Server(budget_bytes=256 << 20, max_inflight=4) as srv:
+    with Server(budget_bytes=256 << 20, max_inflight=4, fused=fused) as srv:
         for a in host + [mix, alone]:
             srv.register(a)
         # the mix: four threads submit concurrently, then wait
@@ -144,15 +145,15 @@ def test_unregistered_host_memory_is_rejected():
         assert srv.lib.bsg_server_register(srv.h, pinned.data_ptr(), 1 << 30) != 0
 
 
-@pytest.mark.parametrize("plain", [False, True])
-def test_short_trace(plain):
+@pytest.mark.parametrize("plain,fused", [(False, False), (False, True), (True, False)])
+def test_short_trace(plain, fused):
     torch = pytest.importorskip("torch")
     pool_n = 1 << 20
     _, host = pinned_book(torch, pool_n, 46)
     out = pinned_zeros(torch, pool_n)
     lat = np.zeros(5000)
     res = serve_trace(host, out, rate_per_s=1000, duration_s=0.5, min_n=16, max_n=1 << 16,
-                      seed=3, budget_bytes=1 << 30, plain=plain, latencies=lat)
+                      seed=3, budget_bytes=1 << 30, plain=plain, latencies=lat, fused=fused)
     assert res["requests"] > 300
     assert res["completed"] == res["requests"]
     assert 0 < res["p50_s"] <= res["p99_s"] <= res["max_s"] < 10
