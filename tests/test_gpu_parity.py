@@ -3,7 +3,7 @@ oracle and the reference's golden outputs.
 
 Tolerances (FP32 output):
   * fast (production) vs the FP64 oracle: max |err| <= 1e-4 on the plain
-    distribution (the spec gate; the reference itself reaches ~8e-5),
+    distribution (the accuracy gate; the reference itself reaches ~8e-5),
     and <= 2e-4 + 2 ulp(price) on the tails (FP32 cannot resolve 1e-4 above
     2048; the reference reaches 5e-4 there).
   * vs the reference's own FP32 prices: <= 2e-4 (both sides ~1e-4 from FP64).
