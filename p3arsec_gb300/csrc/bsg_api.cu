@@ -51,7 +51,11 @@ struct GraphEntry {
     cudaGraphExec_t exec;
 };
 
+// Flag bits the map entry points accept.
+constexpr unsigned kMapFlags = BSG_DEVICE_PTRS | BSG_ASYNC | BSG_MODE_MASK | BSG_NO_GRAPH;
+
 int mode_of(unsigned flags) {
+    if (flags & ~kMapFlags) return -1;
     switch (flags & BSG_MODE_MASK) {
         case BSG_MODE_FAST: return bsg::MODE_FAST;
         case BSG_MODE_SFU_REF: return bsg::MODE_SFU_REF;

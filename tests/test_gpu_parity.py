@@ -220,3 +220,41 @@ def test_bulk_staged_path_bits_and_tails(gpu_ctx, n):
                 assert np.array_equal(got.view(np.uint32), base.view(np.uint32)), (lp, pdl)
     finally:
         gpu_ctx.set_tune(**saved)
+
+
+def test_concurrent_threads_share_a_context_and_own_contexts(gpu_ctx):
+    """Calls on one context are serialised by its lock; separate contexts run
+    side by side.  Every thread gets the bits a lone call gets."""
+    import threading
+    from p3arsec_gb300 import Context
+    book = books.generate(200003, seed=91)
+    want = gpu_ctx.price_book(book)
+    errors = []
+
+    def worker(ctx):
+        try:
+            for _ in range(5):
+                got = ctx.price_book(book, num_runs=2)
+                if not np.array_equal(got.view(np.uint32), want.view(np.uint32)):
+                    errors.append("mismatch")
+        except Exception as e:  # noqa: BLE001
+            errors.append(repr(e))
+
+    own = [Context(0, 1 << 18) for _ in range(2)]
+    threads = [threading.Thread(target=worker, args=(c,)) for c in [gpu_ctx] * 3 + own]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for c in own:
+        c.close()
+    assert not errors, errors
+
+
+def test_unknown_flag_bits_are_rejected(gpu_ctx):
+    from p3arsec_gb300.abi import BsgError
+    book = books.generate(100, seed=92)
+    out = np.zeros(100, dtype=np.float32)
+    st = gpu_ctx.lib.bsg_price_soa(gpu_ctx.h, *[a.ctypes.data for a in book.arrays()],
+                                   out.ctypes.data, 100, 1, 0x8000)
+    assert st == -1
