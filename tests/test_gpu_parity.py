@@ -252,7 +252,6 @@ def test_concurrent_threads_share_a_context_and_own_contexts(gpu_ctx):
 
 
 def test_unknown_flag_bits_are_rejected(gpu_ctx):
-    from p3arsec_gb300.abi import BsgError
     book = books.generate(100, seed=92)
     out = np.zeros(100, dtype=np.float32)
     st = gpu_ctx.lib.bsg_price_soa(gpu_ctx.h, *[a.ctypes.data for a in book.arrays()],
