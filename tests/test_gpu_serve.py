@@ -47,7 +47,8 @@ def test_each_result_same_alone_and_in_mix(gpu_ctx, fused):
     with Server(budget_bytes=256 << 20, max_inflight=4, fused=fused) as srv:
         for a in host + [mix, alone]:
             srv.register(a)
-        # the mix: four threads submit concurrently, then wait
+        # the mix: four threads submit concurrently while admission is held,
+        # so the loop coalesces them into shared batches when it resumes
         ids = [None] * len(reqs)
 
         def client(part):
@@ -55,17 +56,20 @@ def test_each_result_same_alone_and_in_mix(gpu_ctx, fused):
                 o, n = reqs[i]
                 ids[i] = srv.submit(*[a[o:] for a in host], mix[o:], n=n)
 
+        srv.pause(True)
         th = [threading.Thread(target=client, args=(range(j, len(reqs), 4),)) for j in range(4)]
         for t in th:
             t.start()
         for t in th:
             t.join()
+        srv.pause(False)
         for rid in ids:
             st, lat = srv.wait(rid, timeout_s=60.0)
             assert st == OK and lat > 0
         stats = srv.stats()
         assert stats["completed"] == len(reqs)
-        assert stats["batches"] < len(reqs)  # requests were coalesced
+        assert stats["batches"] < len(reqs) / 4  # requests were coalesced
+        assert stats["max_batch_requests_seen"] > 10
         # alone: one request in flight at a time
         for o, n in reqs[:50]:
             st, _ = srv.wait(srv.submit(*[a[o:] for a in host], alone[o:], n=n), timeout_s=60.0)
