@@ -305,6 +305,7 @@ def run_batch(args, rank, world, local):
         ctx.autotune(1 << 16)  # plain per-book launches are small
     stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{local}")
     runs = args.runs
+    batch_tune = ctx.autotune_batch(dev, out_b, pool_len, segs)
 
     def timed(fn):
         for _ in range(args.warmup):
@@ -339,7 +340,7 @@ def run_batch(args, rank, world, local):
         "config": {"workload": f"{args.books} books, sizes log-uniform in [1, 2^20], "
                                f"{total} options, {runs} passes per step",
                    "books": args.books, "options": total, "num_runs": runs,
-                   "tune_plain": ctx.get_tune()},
+                   "tune_plain": ctx.get_tune(), "tune_batch": batch_tune},
         "plain_per_book": {"value": plain, "unit": UNIT, "ms_per_step": 1e3 * secs_p / args.steps,
                            "gpu_launches": launches_p},
         "speedup_vs_plain": value / plain,

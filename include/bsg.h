@@ -132,6 +132,24 @@ int bsg_price_batch(bsg_ctx* ctx, const float* sptprice, const float* strike,
                     size_t pool_len, const bsg_segment* segs, size_t nseg,
                     int num_runs, unsigned flags);
 
+/* Shape of the persistent batch kernel: options per tile handed out by the
+ * work counter, and resident blocks per SM (0 = as many as fit). */
+typedef struct bsg_batch_tune {
+    uint64_t tile_options;
+    int blocks_per_sm;
+} bsg_batch_tune;
+
+/* Times the batch kernel's shapes (tile 2048..32768 options x 1..max blocks
+ * per SM) on these books (one pass each, prices written) and makes the
+ * fastest the context's choice. */
+int bsg_autotune_batch(bsg_ctx* ctx, const float* sptprice, const float* strike,
+                       const float* rate, const float* volatility,
+                       const float* otime, const int32_t* otype, float* prices,
+                       size_t pool_len, const bsg_segment* segs, size_t nseg,
+                       bsg_batch_tune* out);
+int bsg_get_batch_tune(const bsg_ctx* ctx, bsg_batch_tune* out);
+int bsg_set_batch_tune(bsg_ctx* ctx, const bsg_batch_tune* tune);
+
 /* The same books priced by one plain map launch per book (the comparison
  * baseline for bsg_price_batch). */
 int bsg_price_books_plain(bsg_ctx* ctx, const float* sptprice, const float* strike,

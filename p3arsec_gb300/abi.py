@@ -118,6 +118,13 @@ class BookC(ctypes.Structure):
                 ("mem_", ctypes.c_void_p)]
 
 
+class BatchTune(ctypes.Structure):
+    _fields_ = [("tile_options", ctypes.c_uint64), ("blocks_per_sm", ctypes.c_int)]
+
+    def as_dict(self):
+        return {"tile_options": int(self.tile_options), "blocks_per_sm": int(self.blocks_per_sm)}
+
+
 # Every symbol the header declares, with its ctypes signature.
 _P = ctypes.c_void_p
 _SZ = ctypes.c_size_t
@@ -137,6 +144,10 @@ SIGNATURES = {
     "bsg_price_fp64": (_I, [_P] + [_P] * 7 + [_SZ, _U]),
     "bsg_price_soa_f64": (_I, [_P] + [_P] * 7 + [_SZ, _I, _U]),
     "bsg_price_batch": (_I, [_P] + [_P] * 7 + [_SZ, ctypes.POINTER(Segment), _SZ, _I, _U]),
+    "bsg_autotune_batch": (_I, [_P] + [_P] * 7 + [_SZ, ctypes.POINTER(Segment), _SZ,
+                                                  ctypes.POINTER(BatchTune)]),
+    "bsg_get_batch_tune": (_I, [_P, ctypes.POINTER(BatchTune)]),
+    "bsg_set_batch_tune": (_I, [_P, ctypes.POINTER(BatchTune)]),
     "bsg_price_books_plain": (_I, [_P] + [_P] * 7 + [_SZ, ctypes.POINTER(Segment), _SZ, _I, _U]),
     "bsg_price_batch_noalloc": (_I, [_P] * 7 + [_SZ, ctypes.POINTER(Segment), _SZ, _P, _U]),
     "bsg_error_report": (_I, [_P] + [_P] * 7 + [_SZ, _P, _I, ctypes.c_double, ctypes.POINTER(ErrBucket)]),
@@ -310,6 +321,26 @@ class Context:
         st = fn(self.h, *[ptr(x) for x in pool], ptr(prices), pool_len, segs, len(segments),
                 num_runs, flags)
         _check(self.lib, self.h, st)
+
+    def autotune_batch(self, pool, prices, pool_len, segments) -> dict:
+        segs = (Segment * max(len(segments), 1))()
+        for i, (o, l) in enumerate(segments):
+            segs[i].offset = int(o)
+            segs[i].len = int(l)
+        t = BatchTune()
+        st = self.lib.bsg_autotune_batch(self.h, *[ptr(x) for x in pool], ptr(prices), pool_len,
+                                         segs, len(segments), ctypes.byref(t))
+        _check(self.lib, self.h, st)
+        return t.as_dict()
+
+    def set_batch_tune(self, tile_options=8192, blocks_per_sm=0):
+        t = BatchTune(tile_options, blocks_per_sm)
+        _check(self.lib, self.h, self.lib.bsg_set_batch_tune(self.h, ctypes.byref(t)))
+
+    def get_batch_tune(self) -> dict:
+        t = BatchTune()
+        _check(self.lib, self.h, self.lib.bsg_get_batch_tune(self.h, ctypes.byref(t)))
+        return t.as_dict()
 
     def error_report(self, pool, prices, n, edges, rel_floor=1e-3):
         """bsg_error_report over device arrays; returns a list of dicts."""

@@ -41,6 +41,8 @@ struct GraphKey {
     int kind;  // 0 plain map, 1 batch
     uint64_t ntiles;
     int nseg;
+    uint64_t btile;  // batch tile (options) and grid
+    int bgrid;
     bool operator==(const GraphKey& o) const {
         return std::memcmp(this, &o, sizeof(GraphKey)) == 0;
     }
@@ -71,7 +73,9 @@ size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 struct bsg_ctx {
     int device = 0;
     int sm_count = 0;
-    int batch_blocks_per_sm = 1;
+    int batch_blocks_per_sm = 1;  // occupancy limit of the batch kernel
+    uint64_t batch_tile = 8192;   // batch tuning (bsg_autotune_batch)
+    int batch_bps = 0;            // 0 = the occupancy limit
     cudaStream_t stream = nullptr;
     size_t cap = 0;     // max_options
     size_t cap_al = 0;  // per-array stride in the resident buffer
@@ -219,7 +223,8 @@ void graph_put(bsg_ctx* c, const GraphKey& k, cudaGraphExec_t exec) {
 }
 
 GraphKey make_key(const bsg::SoA& a, int64_t n, int runs, int mode,
-                  const bsg::MapCfg& cfg, int kind, uint64_t ntiles, int nseg) {
+                  const bsg::MapCfg& cfg, int kind, uint64_t ntiles, int nseg,
+                  uint64_t btile = 0, int bgrid = 0) {
     GraphKey k;
     std::memset(&k, 0, sizeof(k));  // padding must compare equal
     k.soa = a;
@@ -230,6 +235,8 @@ GraphKey make_key(const bsg::SoA& a, int64_t n, int runs, int mode,
     k.kind = kind;
     k.ntiles = ntiles;
     k.nseg = nseg;
+    k.btile = btile;
+    k.bgrid = bgrid;
     return k;
 }
 
@@ -594,12 +601,15 @@ int bsg_price_soa_f64(bsg_ctx* c, const double* s, const double* k, const double
     return BSG_OK;
 }
 
-int bsg_price_batch(bsg_ctx* c, const float* s, const float* k, const float* r,
-                    const float* v, const float* t, const int32_t* otype,
-                    float* prices, size_t pool_len, const bsg_segment* segs,
-                    size_t nseg, int num_runs, unsigned flags) {
-    if (!c) return BSG_ERR_INVALID_ARG;
-    std::lock_guard<std::mutex> lk(c->mu);
+}  // extern "C"
+
+namespace {
+
+// bsg_price_batch without the lock (the caller holds c->mu).
+int price_batch_impl(bsg_ctx* c, const float* s, const float* k, const float* r,
+                     const float* v, const float* t, const int32_t* otype, float* prices,
+                     size_t pool_len, const bsg_segment* segs, size_t nseg, int num_runs,
+                     unsigned flags) {
     try {
         const int mode = mode_of(flags);
         if (mode < 0 || num_runs < 0) return fail(c, BSG_ERR_INVALID_ARG, "bad mode flag or num_runs");
@@ -615,9 +625,13 @@ int bsg_price_batch(bsg_ctx* c, const float* s, const float* k, const float* r,
              reinterpret_cast<uintptr_t>(t) | reinterpret_cast<uintptr_t>(otype) |
              reinterpret_cast<uintptr_t>(prices)) & 15)
             return fail(c, BSG_ERR_MISALIGNED, "batch pool arrays must be 16-byte aligned");
+        const uint64_t topt = c->batch_tile;
+        const int bps = (c->batch_bps > 0 && c->batch_bps < c->batch_blocks_per_sm)
+                            ? c->batch_bps : c->batch_blocks_per_sm;
+        const int grid = c->sm_count * bps;
         int m = 0;
         uint64_t ntiles = 0;
-        if ((st = build_segments(c, segs, nseg, pool_len, bsg::batch_tile_options(), &m, &ntiles))) return st;
+        if ((st = build_segments(c, segs, nseg, pool_len, topt, &m, &ntiles))) return st;
         if (m == 0) return finish(c, flags);
         const uint64_t* d_off = c->d_seg;
         const uint64_t* d_len = c->d_seg + c->seg_cap;
@@ -627,8 +641,6 @@ int bsg_price_batch(bsg_ctx* c, const float* s, const float* k, const float* r,
         BSG_CK(c, cudaMemcpyAsync((void*)d_len, c->h_seg + c->seg_cap, m * 8, cudaMemcpyHostToDevice, c->stream));
         BSG_CK(c, cudaMemcpyAsync((void*)d_pre, c->h_seg + 2 * c->seg_cap, (m + 1) * 8, cudaMemcpyHostToDevice, c->stream));
         BSG_CK(c, cudaEventRecord(c->seg_ev, c->stream));
-        const int grid = c->sm_count * c->batch_blocks_per_sm;
-        const uint64_t topt = bsg::batch_tile_options();
         // one work counter per pass, zeroed together, so that pass j + 1 can
         // start (PDL) while pass j drains
         if ((size_t)num_runs > c->cursor_cap) {
@@ -653,7 +665,8 @@ int bsg_price_batch(bsg_ctx* c, const float* s, const float* k, const float* r,
             c->launches += (uint64_t)num_runs;
             return finish(c, flags);
         }
-        GraphKey key = make_key(a, (int64_t)pool_len, num_runs, mode, c->tune, 1, ntiles, m);
+        GraphKey key = make_key(a, (int64_t)pool_len, num_runs, mode, c->tune, 1, ntiles, m,
+                                topt, grid);
         cudaGraphExec_t exec = graph_find(c, key);
         if (!exec) {
             cudaGraph_t g = nullptr;
@@ -676,6 +689,86 @@ int bsg_price_batch(bsg_ctx* c, const float* s, const float* k, const float* r,
     } catch (const std::bad_alloc&) {
         return fail(c, BSG_ERR_OUT_OF_MEMORY, "host allocation failed");
     }
+}
+
+}  // namespace
+
+extern "C" {
+
+int bsg_price_batch(bsg_ctx* c, const float* s, const float* k, const float* r,
+                    const float* v, const float* t, const int32_t* otype,
+                    float* prices, size_t pool_len, const bsg_segment* segs,
+                    size_t nseg, int num_runs, unsigned flags) {
+    if (!c) return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mu);
+    return price_batch_impl(c, s, k, r, v, t, otype, prices, pool_len, segs, nseg, num_runs, flags);
+}
+
+int bsg_autotune_batch(bsg_ctx* c, const float* s, const float* k, const float* r,
+                       const float* v, const float* t, const int32_t* otype, float* prices,
+                       size_t pool_len, const bsg_segment* segs, size_t nseg,
+                       bsg_batch_tune* out) {
+    if (!c) return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mu);
+    BSG_CK(c, cudaSetDevice(c->device));
+    cudaEvent_t e0, e1;
+    BSG_CK(c, cudaEventCreate(&e0));
+    BSG_CK(c, cudaEventCreate(&e1));
+    const uint64_t keep_tile = c->batch_tile;
+    const int keep_bps = c->batch_bps;
+    float best_ms = 1e30f;
+    bsg_batch_tune best{keep_tile, keep_bps};
+    int st = BSG_OK;
+    for (uint64_t tile : {2048ull, 4096ull, 8192ull, 16384ull, 32768ull}) {
+        for (int bps = 1; bps <= c->batch_blocks_per_sm && st == BSG_OK; ++bps) {
+            c->batch_tile = tile;
+            c->batch_bps = bps;
+            const unsigned f = BSG_DEVICE_PTRS | BSG_ASYNC;
+            st = price_batch_impl(c, s, k, r, v, t, otype, prices, pool_len, segs, nseg, 1, f);
+            if (st) break;
+            cudaEventRecord(e0, c->stream);
+            for (int i = 0; i < 3 && st == BSG_OK; ++i)
+                st = price_batch_impl(c, s, k, r, v, t, otype, prices, pool_len, segs, nseg, 1, f);
+            cudaEventRecord(e1, c->stream);
+            if (st) break;
+            cudaEventSynchronize(e1);
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = bsg_batch_tune{tile, bps};
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st) {
+        c->batch_tile = keep_tile;
+        c->batch_bps = keep_bps;
+        return st;
+    }
+    BSG_CK(c, cudaStreamSynchronize(c->stream));
+    c->batch_tile = best.tile_options;
+    c->batch_bps = best.blocks_per_sm;
+    if (out) *out = best;
+    return BSG_OK;
+}
+
+int bsg_get_batch_tune(const bsg_ctx* c, bsg_batch_tune* out) {
+    if (!c || !out) return BSG_ERR_INVALID_ARG;
+    out->tile_options = c->batch_tile;
+    out->blocks_per_sm = c->batch_bps;
+    return BSG_OK;
+}
+
+int bsg_set_batch_tune(bsg_ctx* c, const bsg_batch_tune* t) {
+    if (!c || !t || t->tile_options < 256 || t->tile_options > (1ull << 24) ||
+        t->blocks_per_sm < 0 || t->blocks_per_sm > 64)
+        return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->batch_tile = t->tile_options;
+    c->batch_bps = t->blocks_per_sm;
+    return BSG_OK;
 }
 
 int bsg_price_books_plain(bsg_ctx* c, const float* s, const float* k, const float* r,

@@ -101,3 +101,28 @@ def test_error_report_matches_cpu(gpu_ctx, dist):
     assert sum(b["sum_sq_abs"] for b in rep) == pytest.approx((err ** 2).sum(), rel=1e-6)
     if dist == "plain":
         assert max(b["max_abs"] for b in rep) <= 1e-4
+
+
+def test_batch_autotune_and_every_shape_gives_the_same_bits(gpu_ctx):
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(11)
+    segs, pool_len = layout(rng.integers(1, 70000, 120), rng)
+    book = books.generate(pool_len, seed=12)
+    pool = pool_on_device(torch, book)
+    out = torch.zeros(pool_len, device="cuda:0")
+    saved = gpu_ctx.get_batch_tune()
+    try:
+        chosen = gpu_ctx.autotune_batch(pool, out, pool_len, segs)
+        assert chosen["tile_options"] in (2048, 4096, 8192, 16384, 32768)
+        ref = gpu_ctx.price_book(book)
+        for tile in (2048, 32768):
+            for bps in (1, 0):
+                gpu_ctx.set_batch_tune(tile, bps)
+                out.zero_()
+                gpu_ctx.price_batch(pool, out, pool_len, segs, num_runs=2)
+                torch.cuda.synchronize()
+                got = out.cpu().numpy()
+                for o, l in segs:
+                    assert np.array_equal(got[o:o + l].view(np.uint32), ref[o:o + l].view(np.uint32))
+    finally:
+        gpu_ctx.set_batch_tune(**saved)
