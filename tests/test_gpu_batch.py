@@ -106,7 +106,7 @@ def test_error_report_matches_cpu(gpu_ctx, dist):
 def test_batch_autotune_and_every_shape_gives_the_same_bits(gpu_ctx):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(11)
-    segs, pool_len = layout(rng.integers(1, 70000, 120), rng)
+    segs, pool_len = layout(rng.integers(1, 30000, 120), rng)
     book = books.generate(pool_len, seed=12)
     pool = pool_on_device(torch, book)
     out = torch.zeros(pool_len, device="cuda:0")
