@@ -228,15 +228,31 @@ def run_ours(args, rank, world, local):
     if not args.no_e2e:
         host = [torch.from_numpy(a).pin_memory().numpy() for a in book.arrays()]
         hout = torch.empty(n, dtype=torch.float32).pin_memory().numpy()
+        # synchronous calls: each step's copies in series with its passes
         ctx.price_soa(*host, hout, n=n, num_runs=runs)  # warm (graph for the resident buffers)
         barrier(dist, local)
         t0 = time.perf_counter()
         for _ in range(args.steps):
             ctx.price_soa(*host, hout, n=n, num_runs=runs)
+        sync_s = reduce_max(dist, time.perf_counter() - t0, local)
+        # pipelined calls (BSG_ASYNC with host pointers): step k + 1's inputs
+        # cross the host link while step k's passes run; every step still
+        # copies its 240 MB in and 40 MB out inside the timed region
+        for _ in range(2):  # warm both resident sets
+            ctx.price_soa(*host, hout, n=n, num_runs=runs, asynchronous=True)
+        ctx.synchronize()
+        barrier(dist, local)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            ctx.price_soa(*host, hout, n=n, num_runs=runs, asynchronous=True)
+        ctx.synchronize()
         e2e_s = reduce_max(dist, time.perf_counter() - t0, local)
         e2e = {"value": world * n * runs * args.steps / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": 24 * n, "d2h_bytes_per_step": 4 * n,
-               "ms_per_step": 1e3 * e2e_s / args.steps}
+               "ms_per_step": 1e3 * e2e_s / args.steps,
+               "mode": "pipelined bsg_price_soa(BSG_ASYNC, pinned host arrays) + bsg_synchronize",
+               "synchronous": {"value": world * n * runs * args.steps / sync_s,
+                               "ms_per_step": 1e3 * sync_s / args.steps}}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,

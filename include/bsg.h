@@ -51,7 +51,7 @@ typedef enum bsg_status {
 /* ---- flags ------------------------------------------------------------ */
 #define BSG_HOST_PTRS     0x000u /* host arrays: copied in and out inside the call */
 #define BSG_DEVICE_PTRS   0x001u /* device arrays on the context's device */
-#define BSG_ASYNC         0x002u /* device pointers only: return once enqueued */
+#define BSG_ASYNC         0x002u /* return once enqueued (see bsg_price_soa) */
 #define BSG_MODE_FAST     0x000u /* compensated FP32 with SFU approximations */
 #define BSG_MODE_SFU_REF  0x010u /* reference operation order, SFU approximations */
 #define BSG_MODE_LIBM_REF 0x020u /* reference operation order, accurate libm / IEEE */
@@ -71,6 +71,8 @@ const char* bsg_strerror(int status);
 const char* bsg_last_error(const bsg_ctx* ctx);
 /* The context's cudaStream_t (as void*): work of every call is ordered on it. */
 void* bsg_stream(bsg_ctx* ctx);
+/* Waits for every call enqueued on the context (pipelined host calls too). */
+int bsg_synchronize(bsg_ctx* ctx);
 /* Number of kernels this context has launched so far. */
 uint64_t bsg_kernel_launches(const bsg_ctx* ctx);
 
@@ -84,7 +86,12 @@ void bsg_host_free(void* p);
  * num_runs times (each run a full pass over the n options, as the
  * reference's NUM_RUNS loop, blackscholes.c:315-348 / 607-658).
  * Replaces bs_thread (blackscholes.c:607) and the FastFlow map's svc
- * (blackscholes.c:316-346).  n == 0 or num_runs == 0 is a no-op. */
+ * (blackscholes.c:316-346).  n == 0 or num_runs == 0 is a no-op.
+ * BSG_ASYNC with device pointers: returns once enqueued on bsg_stream().
+ * BSG_ASYNC with host pointers (pipelined): returns once enqueued; successive
+ * calls alternate between two resident buffer sets and overlap one call's
+ * host<->device copies with another's passes.  The caller keeps the host
+ * arrays (pinned, for real overlap) unchanged until bsg_synchronize. */
 int bsg_price_soa(bsg_ctx* ctx, const float* sptprice, const float* strike,
                   const float* rate, const float* volatility,
                   const float* otime, const int32_t* otype, float* prices,

@@ -136,6 +136,7 @@ SIGNATURES = {
     "bsg_strerror": (ctypes.c_char_p, [_I]),
     "bsg_last_error": (ctypes.c_char_p, [_P]),
     "bsg_stream": (_P, [_P]),
+    "bsg_synchronize": (_I, [_P]),
     "bsg_kernel_launches": (ctypes.c_uint64, [_P]),
     "bsg_host_alloc": (_P, [_SZ]),
     "bsg_host_free": (None, [_P]),
@@ -252,6 +253,10 @@ class Context:
     @property
     def stream(self) -> int:
         return int(self.lib.bsg_stream(self.h) or 0)
+
+    def synchronize(self):
+        """bsg_synchronize: waits for everything enqueued (pipelined calls too)."""
+        _check(self.lib, self.h, self.lib.bsg_synchronize(self.h))
 
     @property
     def launches(self) -> int:

@@ -95,10 +95,19 @@ struct bsg_ctx {
     // error-report scratch
     bsg::ErrAcc* d_acc = nullptr;
     double* d_edges = nullptr;
+    // pipelined host calls (BSG_ASYNC with host pointers): a second resident
+    // set, copy-in and copy-out streams, and per-set events
+    char* dev_buf2 = nullptr;
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;
+    cudaEvent_t ev_in[2] = {nullptr, nullptr};
+    cudaEvent_t ev_comp[2] = {nullptr, nullptr};
+    cudaEvent_t ev_out[2] = {nullptr, nullptr};
+    int next_set = 0;
+    bool pipelined = false;  // pipelined work may be in flight
 
-    bsg::SoA resident(size_t n) const {
+    bsg::SoA resident(size_t n, int set = 0) const {
         (void)n;
-        float* f = reinterpret_cast<float*>(dev_buf);
+        float* f = reinterpret_cast<float*>(set ? dev_buf2 : dev_buf);
         bsg::SoA a;
         a.s = f;
         a.k = f + cap_al;
@@ -292,6 +301,62 @@ int finish(bsg_ctx* c, unsigned flags) {
     return check_bulk_error(c);
 }
 
+// Waits for pipelined host calls (all three streams).
+int drain_pipeline(bsg_ctx* c) {
+    if (!c->pipelined) return BSG_OK;
+    BSG_CK(c, cudaStreamSynchronize(c->copy_in));
+    BSG_CK(c, cudaStreamSynchronize(c->stream));
+    BSG_CK(c, cudaStreamSynchronize(c->copy_out));
+    c->pipelined = false;
+    return check_bulk_error(c);
+}
+
+int ensure_pipeline(bsg_ctx* c) {
+    if (c->dev_buf2) return BSG_OK;
+    BSG_CK(c, cudaStreamCreateWithFlags(&c->copy_in, cudaStreamNonBlocking));
+    BSG_CK(c, cudaStreamCreateWithFlags(&c->copy_out, cudaStreamNonBlocking));
+    for (int b = 0; b < 2; ++b) {
+        BSG_CK(c, cudaEventCreateWithFlags(&c->ev_in[b], cudaEventDisableTiming));
+        BSG_CK(c, cudaEventCreateWithFlags(&c->ev_comp[b], cudaEventDisableTiming));
+        BSG_CK(c, cudaEventCreateWithFlags(&c->ev_out[b], cudaEventDisableTiming));
+    }
+    BSG_CK(c, cudaMalloc(&c->dev_buf2, 7 * c->cap_al * sizeof(float)));
+    return BSG_OK;
+}
+
+// A pipelined host call: inputs copied into the next of two resident sets on
+// the copy-in stream, the passes on the compute stream, prices copied out on
+// the copy-out stream; events order each set's reuse.  Successive calls
+// overlap one call's copies with another's passes.
+int enqueue_host_pipelined(bsg_ctx* c, const bsg::SoA& h, size_t n, int runs, int mode,
+                           unsigned flags) {
+    int st;
+    if ((st = ensure_pipeline(c))) return st;
+    const int b = c->next_set;
+    c->next_set ^= 1;
+    const bsg::SoA d = c->resident(n, b);
+    const size_t by = n * 4;
+    // this set's inputs may be overwritten once its previous passes are done
+    BSG_CK(c, cudaStreamWaitEvent(c->copy_in, c->ev_comp[b], 0));
+    BSG_CK(c, cudaMemcpyAsync((void*)d.s, h.s, by, cudaMemcpyHostToDevice, c->copy_in));
+    BSG_CK(c, cudaMemcpyAsync((void*)d.k, h.k, by, cudaMemcpyHostToDevice, c->copy_in));
+    BSG_CK(c, cudaMemcpyAsync((void*)d.r, h.r, by, cudaMemcpyHostToDevice, c->copy_in));
+    BSG_CK(c, cudaMemcpyAsync((void*)d.v, h.v, by, cudaMemcpyHostToDevice, c->copy_in));
+    BSG_CK(c, cudaMemcpyAsync((void*)d.t, h.t, by, cudaMemcpyHostToDevice, c->copy_in));
+    BSG_CK(c, cudaMemcpyAsync((void*)d.ot, h.ot, by, cudaMemcpyHostToDevice, c->copy_in));
+    BSG_CK(c, cudaEventRecord(c->ev_in[b], c->copy_in));
+    // the passes need the inputs, and this set's previous prices read out
+    BSG_CK(c, cudaStreamWaitEvent(c->stream, c->ev_in[b], 0));
+    BSG_CK(c, cudaStreamWaitEvent(c->stream, c->ev_out[b], 0));
+    c->pipelined = true;
+    if ((st = enqueue_map_runs(c, d, (int64_t)n, runs, mode, flags))) return st;
+    BSG_CK(c, cudaEventRecord(c->ev_comp[b], c->stream));
+    BSG_CK(c, cudaStreamWaitEvent(c->copy_out, c->ev_comp[b], 0));
+    BSG_CK(c, cudaMemcpyAsync(h.out, d.out, by, cudaMemcpyDeviceToHost, c->copy_out));
+    BSG_CK(c, cudaEventRecord(c->ev_out[b], c->copy_out));
+    return BSG_OK;
+}
+
 int grow_seg_scratch(bsg_ctx* c, size_t nseg) {
     if (nseg <= c->seg_cap) return BSG_OK;
     size_t cap = std::max<size_t>(nseg, 1024);
@@ -423,7 +488,17 @@ int bsg_create(bsg_ctx** out, int device, size_t max_options) {
 void bsg_destroy(bsg_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
+    if (c->copy_in) cudaStreamSynchronize(c->copy_in);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->copy_out) cudaStreamSynchronize(c->copy_out);
+    for (int b = 0; b < 2; ++b) {
+        if (c->ev_in[b]) cudaEventDestroy(c->ev_in[b]);
+        if (c->ev_comp[b]) cudaEventDestroy(c->ev_comp[b]);
+        if (c->ev_out[b]) cudaEventDestroy(c->ev_out[b]);
+    }
+    if (c->copy_in) cudaStreamDestroy(c->copy_in);
+    if (c->copy_out) cudaStreamDestroy(c->copy_out);
+    if (c->dev_buf2) cudaFree(c->dev_buf2);
     graph_drop_all(c);
     if (c->dev_buf) cudaFree(c->dev_buf);
     if (c->d_seg) cudaFree(c->d_seg);
@@ -437,6 +512,16 @@ void bsg_destroy(bsg_ctx* c) {
 }
 
 void* bsg_stream(bsg_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int bsg_synchronize(bsg_ctx* c) {
+    if (!c) return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mu);
+    BSG_CK(c, cudaSetDevice(c->device));
+    int st = drain_pipeline(c);
+    if (st) return st;
+    BSG_CK(c, cudaStreamSynchronize(c->stream));
+    return check_bulk_error(c);
+}
 
 uint64_t bsg_kernel_launches(const bsg_ctx* c) { return c ? c->launches : 0; }
 
@@ -471,9 +556,10 @@ int bsg_price_soa(bsg_ctx* c, const float* s, const float* k, const float* r,
             if ((st = enqueue_map_runs(c, a, (int64_t)n, num_runs, mode, flags))) return st;
             return finish(c, flags);
         }
-        if (flags & BSG_ASYNC) return fail(c, BSG_ERR_INVALID_ARG, "BSG_ASYNC needs device pointers");
         if ((st = check_soa_host(c, a))) return st;
         if (n > c->cap) return fail(c, BSG_ERR_CAPACITY, "n exceeds the context's max_options");
+        if (flags & BSG_ASYNC) return enqueue_host_pipelined(c, a, n, num_runs, mode, flags);
+        if ((st = drain_pipeline(c))) return st;
         const bsg::SoA d = c->resident(n);
         const size_t b = n * 4;
         BSG_CK(c, cudaMemcpyAsync((void*)d.s, s, b, cudaMemcpyHostToDevice, c->stream));

@@ -257,3 +257,25 @@ def test_unknown_flag_bits_are_rejected(gpu_ctx):
     st = gpu_ctx.lib.bsg_price_soa(gpu_ctx.h, *[a.ctypes.data for a in book.arrays()],
                                    out.ctypes.data, 100, 1, 0x8000)
     assert st == -1
+
+
+def test_pipelined_host_calls_equal_synchronous_calls(gpu_ctx):
+    """BSG_ASYNC with host pointers: calls alternate between two resident sets
+    and overlap copies with passes; every result equals a lone call's."""
+    torch = pytest.importorskip("torch")
+    bks = [books.generate(n, seed=100 + i) for i, n in enumerate((300001, 4, 1 << 20, 77777, 1))]
+    want = [gpu_ctx.price_book(b) for b in bks]
+    pinned = [[torch.from_numpy(a).pin_memory().numpy() for a in b.arrays()] for b in bks]
+    outs = [torch.zeros(len(b), dtype=torch.float32).pin_memory().numpy() for b in bks]
+    for rep in range(2):
+        for arrs, out in zip(pinned, outs):
+            gpu_ctx.price_soa(*arrs, out, n=len(out), num_runs=3, asynchronous=True)
+        gpu_ctx.synchronize()
+        for w, o in zip(want, outs):
+            assert np.array_equal(o.view(np.uint32), w.view(np.uint32)), rep
+    # a synchronous call after pipelined ones drains them first
+    gpu_ctx.price_soa(*pinned[0], outs[0], n=len(outs[0]), num_runs=1, asynchronous=True)
+    again = gpu_ctx.price_book(bks[2])
+    assert np.array_equal(again.view(np.uint32), want[2].view(np.uint32))
+    gpu_ctx.synchronize()
+    assert np.array_equal(outs[0].view(np.uint32), want[0].view(np.uint32))
