@@ -64,7 +64,13 @@ typedef enum bsg_status {
 
 /* New context on CUDA device `device` able to price up to max_options per
  * call with host pointers (device-pointer calls have no size limit).
- * Allocates 28 * max_options bytes of device memory. */
+ * Allocates 28 * max_options bytes of device memory.
+ * Debug guards: with the environment variable BSG_DEBUG set (and not "0")
+ * when the context is created, every resident array is followed by at least
+ * 64 guard words; each synchronous call then checks that no kernel or copy
+ * wrote past the options it was given (the resident prices past n included)
+ * and returns BSG_ERR_STATE, naming the first overwritten word, if one did.
+ * Off by default: the check costs a launch and a synchronisation per call. */
 int bsg_create(bsg_ctx** out, int device, size_t max_options);
 void bsg_destroy(bsg_ctx* ctx);
 const char* bsg_strerror(int status);
@@ -385,6 +391,13 @@ int bsg_autotune(bsg_ctx* ctx, size_t n, bsg_tune* out);
  * Expected result: BSG_ERR_TIMEOUT, the context still usable afterwards.
  * elapsed_s (optional): host time of the call. */
 int bsg_selftest_wait_timeout(bsg_ctx* ctx, double limit_s, double* elapsed_s);
+
+/* Self-test of the debug guards (contexts created with BSG_DEBUG set):
+ * overwrites the last guard word after the resident price array (inside the
+ * context's own allocation), runs the post-call check, then restores the
+ * word.  Expected result: BSG_ERR_STATE with the word named by
+ * bsg_last_error(); BSG_ERR_NOT_SUPPORTED without BSG_DEBUG. */
+int bsg_selftest_guard(bsg_ctx* ctx);
 int bsg_get_tune(const bsg_ctx* ctx, bsg_tune* out);
 int bsg_set_tune(bsg_ctx* ctx, const bsg_tune* tune);
 

@@ -174,6 +174,7 @@ SIGNATURES = {
     "bsg_read_soa": (_I, [ctypes.c_char_p, ctypes.POINTER(BookC)]),
     "bsg_autotune": (_I, [_P, _SZ, ctypes.POINTER(Tune)]),
     "bsg_selftest_wait_timeout": (_I, [_P, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+    "bsg_selftest_guard": (_I, [_P]),
     "bsg_get_tune": (_I, [_P, ctypes.POINTER(Tune)]),
     "bsg_set_tune": (_I, [_P, ctypes.POINTER(Tune)]),
 }
@@ -377,6 +378,11 @@ class Context:
         el = ctypes.c_double()
         st = self.lib.bsg_selftest_wait_timeout(self.h, limit_s, ctypes.byref(el))
         return st, el.value
+
+    def selftest_guard(self):
+        """Plants one overwritten debug guard word; returns (status, message)."""
+        st = self.lib.bsg_selftest_guard(self.h)
+        return st, self.lib.bsg_last_error(self.h).decode()
 
     def get_tune(self) -> dict:
         t = Tune()

@@ -68,6 +68,15 @@ int mode_of(unsigned flags) {
 
 size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+constexpr size_t kGuardWords = 64;        // guard words after each resident array
+constexpr int kGuardByte = 0xA5;          // guard fill byte
+constexpr uint32_t kGuardWord = 0xA5A5A5A5u;
+
+bool debug_env() {
+    const char* e = std::getenv("BSG_DEBUG");
+    return e && *e && std::strcmp(e, "0") != 0;
+}
+
 }  // namespace
 
 struct bsg_ctx {
@@ -104,6 +113,11 @@ struct bsg_ctx {
     cudaEvent_t ev_out[2] = {nullptr, nullptr};
     int next_set = 0;
     bool pipelined = false;  // pipelined work may be in flight
+    // debug guards (BSG_DEBUG set at bsg_create): every resident array is
+    // followed by at least kGuardWords words of kGuardByte, checked after
+    // each synchronous call; d_guard holds the check's {count, first index}
+    bool debug = false;
+    unsigned long long* d_guard = nullptr;
 
     bsg::SoA resident(size_t n, int set = 0) const {
         (void)n;
@@ -295,10 +309,54 @@ int check_bulk_error(bsg_ctx* c) {
     return BSG_OK;
 }
 
+// Debug guards: checks that the guard words of both resident sets still hold
+// the fill (set 0's price array from out_lo on, every other array from
+// max_options on) once the context's streams are idle.  A difference means a
+// kernel or a copy wrote past the options it was given: BSG_ERR_STATE, with
+// the first overwritten word.
+int debug_check(bsg_ctx* c, size_t out_lo) {
+    if (!c->debug) return BSG_OK;
+    for (int set = 0; set < 2; ++set) {
+        const char* buf = set ? c->dev_buf2 : c->dev_buf;
+        if (!buf) continue;
+        BSG_CK(c, cudaMemsetAsync(c->d_guard, 0, 8, c->stream));
+        BSG_CK(c, cudaMemsetAsync(c->d_guard + 1, 0xFF, 8, c->stream));
+        cudaError_t e = bsg::launch_guard_check(
+            reinterpret_cast<const uint32_t*>(buf), (int64_t)c->cap_al, (int64_t)c->cap,
+            (int64_t)(set ? c->cap : out_lo), kGuardWord, c->d_guard, c->sm_count, c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "launch_guard_check");
+        c->launches++;
+        unsigned long long h[2] = {0, 0};
+        BSG_CK(c, cudaMemcpyAsync(h, c->d_guard, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+        BSG_CK(c, cudaStreamSynchronize(c->stream));
+        if (h[0]) {
+            static const char* names[7] = {"sptprice", "strike", "rate", "volatility",
+                                           "otime", "otype", "prices"};
+            const size_t arr = (size_t)(h[1] / c->cap_al), off = (size_t)(h[1] % c->cap_al);
+            return fail(c, BSG_ERR_STATE,
+                        "debug guard: " + std::to_string(h[0]) +
+                            " guard word(s) overwritten in resident set " + std::to_string(set) +
+                            "; first: " + names[arr < 7 ? arr : 6] + "[" + std::to_string(off) +
+                            "] (max_options " + std::to_string(c->cap) + ")");
+        }
+    }
+    return BSG_OK;
+}
+
+// Debug guards: refills set 0's price array from n on before a synchronous
+// host call of n options, so that the check after it covers [n, max_options).
+int debug_arm(bsg_ctx* c, size_t n) {
+    if (!c->debug) return BSG_OK;
+    float* out = reinterpret_cast<float*>(c->dev_buf) + 6 * c->cap_al;
+    BSG_CK(c, cudaMemsetAsync(out + n, kGuardByte, (c->cap_al - n) * 4, c->stream));
+    return BSG_OK;
+}
+
 int finish(bsg_ctx* c, unsigned flags) {
     if (flags & BSG_ASYNC) return BSG_OK;
     BSG_CK(c, cudaStreamSynchronize(c->stream));
-    return check_bulk_error(c);
+    int st = check_bulk_error(c);
+    return st ? st : debug_check(c, c->cap);
 }
 
 // Waits for pipelined host calls (all three streams).
@@ -308,7 +366,8 @@ int drain_pipeline(bsg_ctx* c) {
     BSG_CK(c, cudaStreamSynchronize(c->stream));
     BSG_CK(c, cudaStreamSynchronize(c->copy_out));
     c->pipelined = false;
-    return check_bulk_error(c);
+    int st = check_bulk_error(c);
+    return st ? st : debug_check(c, c->cap);
 }
 
 int ensure_pipeline(bsg_ctx* c) {
@@ -321,6 +380,11 @@ int ensure_pipeline(bsg_ctx* c) {
         BSG_CK(c, cudaEventCreateWithFlags(&c->ev_out[b], cudaEventDisableTiming));
     }
     BSG_CK(c, cudaMalloc(&c->dev_buf2, 7 * c->cap_al * sizeof(float)));
+    if (c->debug) {
+        // the copy-in stream writes this set next: fill it before returning
+        BSG_CK(c, cudaMemsetAsync(c->dev_buf2, kGuardByte, 7 * c->cap_al * sizeof(float), c->stream));
+        BSG_CK(c, cudaStreamSynchronize(c->stream));
+    }
     return BSG_OK;
 }
 
@@ -467,8 +531,14 @@ int bsg_create(bsg_ctx** out, int device, size_t max_options) {
         if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { rc = BSG_ERR_CUDA; break; }
         if (cudaEventCreateWithFlags(&c->seg_ev, cudaEventDisableTiming) != cudaSuccess) { rc = BSG_ERR_CUDA; break; }
         c->cap = max_options;
-        c->cap_al = round_up(std::max<size_t>(max_options, 1), 64);  // 256-byte aligned arrays
+        c->debug = debug_env();
+        // 256-byte aligned arrays, each followed by guard words in debug mode
+        c->cap_al = round_up(std::max<size_t>(max_options, 1) + (c->debug ? kGuardWords : 0), 64);
         if (cudaMalloc(&c->dev_buf, 7 * c->cap_al * sizeof(float)) != cudaSuccess) { rc = BSG_ERR_OUT_OF_MEMORY; break; }
+        if (c->debug) {
+            if (cudaMalloc(&c->d_guard, 16) != cudaSuccess) { rc = BSG_ERR_OUT_OF_MEMORY; break; }
+            if (cudaMemsetAsync(c->dev_buf, kGuardByte, 7 * c->cap_al * sizeof(float), c->stream) != cudaSuccess) { rc = BSG_ERR_CUDA; break; }
+        }
         c->cursor_cap = 128;
         if (cudaMalloc(&c->d_cursor, c->cursor_cap * 8) != cudaSuccess) { rc = BSG_ERR_OUT_OF_MEMORY; break; }
         if (cudaMalloc(&c->d_acc, sizeof(bsg::ErrAcc) * bsg::kMaxErrBuckets) != cudaSuccess) { rc = BSG_ERR_OUT_OF_MEMORY; break; }
@@ -506,6 +576,7 @@ void bsg_destroy(bsg_ctx* c) {
     if (c->d_cursor) cudaFree(c->d_cursor);
     if (c->d_acc) cudaFree(c->d_acc);
     if (c->d_edges) cudaFree(c->d_edges);
+    if (c->d_guard) cudaFree(c->d_guard);
     if (c->seg_ev) cudaEventDestroy(c->seg_ev);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -520,7 +591,8 @@ int bsg_synchronize(bsg_ctx* c) {
     int st = drain_pipeline(c);
     if (st) return st;
     BSG_CK(c, cudaStreamSynchronize(c->stream));
-    return check_bulk_error(c);
+    if ((st = check_bulk_error(c))) return st;
+    return debug_check(c, c->cap);
 }
 
 uint64_t bsg_kernel_launches(const bsg_ctx* c) { return c ? c->launches : 0; }
@@ -543,6 +615,7 @@ int bsg_price_soa(bsg_ctx* c, const float* s, const float* k, const float* r,
                   float* prices, size_t n, int num_runs, unsigned flags) {
     if (!c) return BSG_ERR_INVALID_ARG;
     std::lock_guard<std::mutex> lk(c->mu);
+    bsg::NvtxRange nvtx_("bsg_price_soa");
     try {
         const int mode = mode_of(flags);
         if (mode < 0 || num_runs < 0) return fail(c, BSG_ERR_INVALID_ARG, "bad mode flag or num_runs");
@@ -560,6 +633,7 @@ int bsg_price_soa(bsg_ctx* c, const float* s, const float* k, const float* r,
         if (n > c->cap) return fail(c, BSG_ERR_CAPACITY, "n exceeds the context's max_options");
         if (flags & BSG_ASYNC) return enqueue_host_pipelined(c, a, n, num_runs, mode, flags);
         if ((st = drain_pipeline(c))) return st;
+        if ((st = debug_arm(c, n))) return st;
         const bsg::SoA d = c->resident(n);
         const size_t b = n * 4;
         BSG_CK(c, cudaMemcpyAsync((void*)d.s, s, b, cudaMemcpyHostToDevice, c->stream));
@@ -571,7 +645,8 @@ int bsg_price_soa(bsg_ctx* c, const float* s, const float* k, const float* r,
         if ((st = enqueue_map_runs(c, d, (int64_t)n, num_runs, mode, flags))) return st;
         BSG_CK(c, cudaMemcpyAsync(prices, d.out, b, cudaMemcpyDeviceToHost, c->stream));
         BSG_CK(c, cudaStreamSynchronize(c->stream));
-        return check_bulk_error(c);
+        if ((st = check_bulk_error(c))) return st;
+        return debug_check(c, n);
     } catch (const std::bad_alloc&) {
         return fail(c, BSG_ERR_OUT_OF_MEMORY, "host allocation failed");
     }
@@ -617,6 +692,8 @@ int bsg_price_fp64(bsg_ctx* c, const float* s, const float* k, const float* r,
     if (!s || !k || !r || !v || !t || !otype || !out)
         return fail(c, BSG_ERR_INVALID_ARG, "a host array is NULL");
     if (n > c->cap) return fail(c, BSG_ERR_CAPACITY, "n exceeds the context's max_options");
+    // the resident set may still be in use by pipelined calls
+    if ((st = drain_pipeline(c))) return st;
     const bsg::SoA d = c->resident(n);
     const size_t b = n * 4;
     double* dout = nullptr;
@@ -633,7 +710,7 @@ int bsg_price_fp64(bsg_ctx* c, const float* s, const float* k, const float* r,
     c->launches++;
     BSG_CK(c, cudaMemcpyAsync(out, dout, n * 8, cudaMemcpyDeviceToHost, c->stream));
     BSG_CK(c, cudaStreamSynchronize(c->stream));
-    return BSG_OK;
+    return debug_check(c, c->cap);
 }
 
 int bsg_price_soa_f64(bsg_ctx* c, const double* s, const double* k, const double* r,
@@ -787,6 +864,7 @@ int bsg_price_batch(bsg_ctx* c, const float* s, const float* k, const float* r,
                     size_t nseg, int num_runs, unsigned flags) {
     if (!c) return BSG_ERR_INVALID_ARG;
     std::lock_guard<std::mutex> lk(c->mu);
+    bsg::NvtxRange nvtx_("bsg_price_batch");
     return price_batch_impl(c, s, k, r, v, t, otype, prices, pool_len, segs, nseg, num_runs, flags);
 }
 
@@ -935,6 +1013,8 @@ int bsg_selftest_wait_timeout(bsg_ctx* c, double limit_s, double* elapsed_s) {
     BSG_CK(c, cudaSetDevice(c->device));
     const size_t n = 4096;  // one tile of the <4, 4> ring per CTA that runs
     if (n > c->cap) return fail(c, BSG_ERR_CAPACITY, "context too small for the self-test");
+    int st = drain_pipeline(c);
+    if (st) return st;
     bsg::bulk_error_take();
     const bsg::SoA d = c->resident(n);
     cudaError_t e = bsg::launch_fill(d, (int64_t)n, 7u, c->sm_count, c->stream);
@@ -950,6 +1030,22 @@ int bsg_selftest_wait_timeout(bsg_ctx* c, double limit_s, double* elapsed_s) {
     if (bsg::bulk_error_take())
         return fail(c, BSG_ERR_TIMEOUT, "the staged kernel's bounded wait expired (self-test)");
     return BSG_OK;
+}
+
+int bsg_selftest_guard(bsg_ctx* c) {
+    if (!c) return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (!c->debug) return fail(c, BSG_ERR_NOT_SUPPORTED, "the context was created without BSG_DEBUG");
+    BSG_CK(c, cudaSetDevice(c->device));
+    int st = drain_pipeline(c);
+    if (st) return st;
+    // the last word of set 0's price array: a guard word (cap_al >= cap + 64)
+    uint32_t* w = reinterpret_cast<uint32_t*>(c->dev_buf) + 7 * c->cap_al - 1;
+    BSG_CK(c, cudaMemsetAsync(w, 0x5A, 4, c->stream));
+    st = debug_check(c, c->cap);
+    BSG_CK(c, cudaMemsetAsync(w, kGuardByte, 4, c->stream));
+    BSG_CK(c, cudaStreamSynchronize(c->stream));
+    return st;
 }
 
 int bsg_get_tune(const bsg_ctx* c, bsg_tune* out) {
@@ -1024,6 +1120,7 @@ static void tune_cache_store(const std::string& key, const bsg_tune& t) {
 extern "C" int bsg_autotune(bsg_ctx* c, size_t n, bsg_tune* out) {
     if (!c || n == 0) return BSG_ERR_INVALID_ARG;
     std::lock_guard<std::mutex> lk(c->mu);
+    bsg::NvtxRange nvtx_("bsg_autotune");
     BSG_CK(c, cudaSetDevice(c->device));
     const std::string key = tune_key(c, n);
     bsg_tune best{};
@@ -1032,6 +1129,7 @@ extern "C" int bsg_autotune(bsg_ctx* c, size_t n, bsg_tune* out) {
         if (out) *out = best;
         return BSG_OK;
     }
+    if (int st = drain_pipeline(c)) return st;
     // inputs: the resident buffers when they fit, else a temporary pool
     bsg::SoA a;
     char* tmp = nullptr;

@@ -2,6 +2,7 @@
 // kernels (bsg_kernels.cu).  Not installed; no torch types anywhere.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 namespace bsg {
@@ -94,8 +95,26 @@ cudaError_t launch_err_report(const SoA& a, const float* prices, int64_t n,
                               double rel_floor, ErrAcc* acc, int sm_count,
                               cudaStream_t st);
 
+// NVTX range for the lifetime of a scope (header-only NVTX3: a no-op unless a
+// profiler injects itself), so profiler timelines show the library's calls.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
 // Fills n options with a deterministic plausible book (autotuning input).
 cudaError_t launch_fill(const SoA& a, int64_t n, uint32_t seed, int sm_count,
                         cudaStream_t st);
+
+// Debug guards of a resident set: seven arrays of `stride` words from `base`;
+// the guard of input array a < 6 is words [cap, stride), that of the price
+// array words [out_lo, stride).  Adds the number of guard words that differ
+// from `pattern` to res[0] and lowers res[1] to the smallest differing word's
+// index from `base` (res must hold {0, ~0} beforehand).
+cudaError_t launch_guard_check(const uint32_t* base, int64_t stride, int64_t cap,
+                               int64_t out_lo, uint32_t pattern, unsigned long long* res,
+                               int sm_count, cudaStream_t st);
 
 }  // namespace bsg

@@ -697,4 +697,39 @@ cudaError_t launch_fill(const SoA& a, int64_t n, uint32_t seed, int sm_count,
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Debug guards (contexts created with BSG_DEBUG set): one CTA row per array.
+
+__global__ void guard_check_kernel(const uint32_t* __restrict__ base, int64_t stride,
+                                   int64_t cap, int64_t out_lo, uint32_t pattern,
+                                   unsigned long long* res) {
+    const int64_t a = blockIdx.y;
+    const int64_t lo = a == 6 ? out_lo : cap;
+    unsigned long long cnt = 0, first = ~0ull;
+    for (int64_t i = lo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < stride;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        if (base[a * stride + i] != pattern) {
+            ++cnt;
+            first = min(first, (unsigned long long)(a * stride + i));
+        }
+    }
+    if (cnt) {
+        atomicAdd(&res[0], cnt);
+        atomicMin(&res[1], first);
+    }
+}
+
+cudaError_t launch_guard_check(const uint32_t* base, int64_t stride, int64_t cap,
+                               int64_t out_lo, uint32_t pattern, unsigned long long* res,
+                               int sm_count, cudaStream_t st) {
+    if (cap > stride || out_lo > stride || cap < 0 || out_lo < 0) return cudaErrorInvalidValue;
+    const int64_t span = stride - (cap < out_lo ? cap : out_lo);
+    int64_t gx = (span + 255) / 256;
+    if (gx > 4LL * sm_count) gx = 4LL * sm_count;
+    if (gx < 1) gx = 1;
+    guard_check_kernel<<<dim3((unsigned)gx, 7), 256, 0, st>>>(base, stride, cap, out_lo,
+                                                              pattern, res);
+    return cudaGetLastError();
+}
+
 }  // namespace bsg

@@ -332,6 +332,7 @@ struct bsg_server {
 
     // --------------------------------------------------------- enqueue
     int enqueue_batched(Slot& sl) {
+        bsg::NvtxRange nvtx_("bsg_server batch");
         const int m = (int)sl.reqs.size();
         Desc* hd = reinterpret_cast<Desc*>(sl.h_tab);
         uint64_t* hoff = reinterpret_cast<uint64_t*>(sl.h_tab + (size_t)m * sizeof(Desc));
@@ -379,6 +380,7 @@ struct bsg_server {
     }
 
     int enqueue_plain(Slot& sl) {
+        bsg::NvtxRange nvtx_("bsg_server plain request");
         const Request* q = sl.reqs[0];
         const uint64_t o = q->off;
         const size_t b = q->r.n * 4;
