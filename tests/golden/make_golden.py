@@ -7,7 +7,8 @@ by oracle/Makefile into oracle/_ref/):
 
 For each seeded case it stores the float32 inputs, the prices of the
 reference's own BlkSchlsEqEuroNoDiv (bits), and the FP64 same-formula oracle,
-and it runs the reference CLI (serial, FastFlow, OpenMP builds) on the PARSEC
+and it runs the reference CLI (serial, FastFlow, OpenMP and SkePU2-OpenMP
+builds) on the PARSEC
 text file and records the SHA-256 of each output file and the ERR_CHK count
 against an FP64-filled DGrefval column.  Fixtures are small (.npz + .json).
 """
@@ -96,7 +97,7 @@ def main():
             inp = os.path.join(td, "in.txt")
             books.write_parsec_input(inp, book, dgrefval=fp64)
             for binary, nthr in (("blackscholes_serial", 1), ("blackscholes_ff", 4),
-                                 ("blackscholes_omp", 4)):
+                                 ("blackscholes_omp", 4), ("blackscholes_skepu_omp", 4)):
                 out = os.path.join(td, f"{binary}.txt")
                 run_cli(binary, nthr, inp, out)
                 info["cli"][f"{binary}:{nthr}"] = sha256(out)
