@@ -34,12 +34,14 @@ BYTES_PER_OPTION = 28  # 5 float inputs + int32 otype + float price
 METRIC = "options/sec & %HBM roofline"
 UNIT = "options/s"
 SEED = 20241203
-# Steady-state DRAM bytes per option per pass of the fast map kernel by load
-# path, from warm ncu captures (dram__bytes_read.sum + dram__bytes_write.sum
-# of mid-run 10M-option launches / 10M) summarised in
-# profiles/map_fast_10M.md; traffic grows in proportion to the options of a
-# launch.  Shapes not captured report null.
-NCU_DRAM_BYTES_PER_OPTION = {1: 20.60, 2: 26.61}
+# Steady-state DRAM bytes per pass of the fast map kernel by (load path,
+# options), from warm ncu captures (dram__bytes_read.sum +
+# dram__bytes_write.sum of mid-run launches) summarised in
+# profiles/map_fast_10M.md.  The L2 keeps a fixed slice of the working set
+# between passes, so traffic is not proportional to the options: sizes and
+# shapes not captured report null.
+NCU_DRAM_BYTES_PER_PASS = {(1, 10_000_000): 206.0e6, (2, 10_000_000): 266.1e6,
+                           (6, 10_000_000): 206.9e6}
 NCU_PROFILE = "profiles/map_fast_10M.md"
 
 
@@ -262,14 +264,17 @@ def run_ours(args, rank, world, local):
         "config": {"workload": f"plain map, {n} European options FP32 SoA, NUM_RUNS={runs} "
                                "passes per step", "options": n, "num_runs": runs,
                    "parallelism": f"replicas x{world} (independent books)",
-                   "l2": "inputs (280 MB) larger than L2 (129 MB); no flush",
+                   "l2": (f"inputs ({BYTES_PER_OPTION * n / 1e6:.0f} MB) larger than L2 "
+                          "(129 MB); no flush" if BYTES_PER_OPTION * n > 129e6 else
+                          f"inputs ({BYTES_PER_OPTION * n / 1e6:.1f} MB) fit in L2 (129 MB): "
+                          "an L2-resident run, not an HBM measurement"),
                    "tune": tune, "mode": "fast"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src,
-                     "traffic": (NCU_DRAM_BYTES_PER_OPTION[tune["load_path"]] * n
-                                 if tune["load_path"] in NCU_DRAM_BYTES_PER_OPTION else None),
+                     "traffic": NCU_DRAM_BYTES_PER_PASS.get((tune["load_path"], n)),
                      "traffic_source": (NCU_PROFILE + " (warm, steady state)"
-                                        if tune["load_path"] in NCU_DRAM_BYTES_PER_OPTION else None),
+                                        if (tune["load_path"], n) in NCU_DRAM_BYTES_PER_PASS
+                                        else None),
                      "bytes_per_launch": BYTES_PER_OPTION * n,
                      "avg_launch_us": per_launch_s * 1e6},
         "accuracy": accuracy,

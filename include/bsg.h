@@ -378,7 +378,8 @@ typedef struct bsg_tune {
                            3, 4, 5 = TMA bulk copies into a shared-memory
                                ring of 3 x 48 KB (1 CTA per SM), 4 x 24 KB
                                (2 per SM) or 3 x 24 KB (3 per SM); block and
-                               grid are then fixed */
+                               grid are then fixed,
+                           6 = LDG.256 evict-first (vec_per_thread 1 or 2) */
     int pdl;            /* 1 = programmatic dependent launch between passes */
 } bsg_tune;
 

@@ -304,7 +304,7 @@ int enqueue_map_runs(bsg_ctx* c, const bsg::SoA& a, int64_t n, int runs, int mod
 // The bulk-staged kernel reports an expired wait in an error word; any call
 // that synchronises checks it.
 int check_bulk_error(bsg_ctx* c) {
-    if (c->tune.load_path >= 3 && bsg::bulk_error_take())
+    if (c->tune.load_path >= 3 && c->tune.load_path <= 5 && bsg::bulk_error_take())
         return fail(c, BSG_ERR_TIMEOUT, "a bulk-copy wait of the staged map kernel expired");
     return BSG_OK;
 }
@@ -1060,10 +1060,10 @@ int bsg_get_tune(const bsg_ctx* c, bsg_tune* out) {
 
 static bool tune_valid(const bsg_tune* t) {
     const bool vpt_ok = t->vec_per_thread == 1 || t->vec_per_thread == 2 ||
-                        (t->vec_per_thread == 4 && t->load_path != 2);
+                        (t->vec_per_thread == 4 && t->load_path < 2);
     const bool blk_ok = t->block == 128 || t->block == 256 || t->block == 512;
     return vpt_ok && blk_ok && t->blocks_per_sm >= 0 && t->blocks_per_sm <= 64 &&
-           t->load_path >= 0 && t->load_path <= 5 && (t->pdl == 0 || t->pdl == 1);
+           t->load_path >= 0 && t->load_path <= 6 && (t->pdl == 0 || t->pdl == 1);
 }
 
 int bsg_set_tune(bsg_ctx* c, const bsg_tune* t) {
@@ -1149,55 +1149,63 @@ extern "C" int bsg_autotune(bsg_ctx* c, size_t n, bsg_tune* out) {
     cudaEvent_t e0, e1;
     BSG_CK(c, cudaEventCreate(&e0));
     BSG_CK(c, cudaEventCreate(&e1));
-    float best_ms = 1e30f;
-    const int reps = 5;  // back to back, as the NUM_RUNS passes run
-    for (int lp = 0; lp <= 2; ++lp)
-        for (int vpt : {1, 2, 4})
-            for (int block : {128, 256, 512})
-                for (int bps : {0, 2, 4, 8})
-                for (int pdl : {0, 1}) {
-                    bsg_tune t{vpt, block, bps, lp, pdl};
-                    if (!tune_valid(&t)) continue;
-                    const bsg::MapCfg cfg{vpt, block, bps, lp, pdl};
-                    e = bsg::launch_map(a, (int64_t)n, bsg::MODE_FAST, cfg, c->sm_count, c->stream);
-                    if (e != cudaSuccess) break;
-                    cudaEventRecord(e0, c->stream);
-                    for (int i = 0; i < reps && e == cudaSuccess; ++i)
-                        e = bsg::launch_map(a, (int64_t)n, bsg::MODE_FAST, cfg, c->sm_count, c->stream);
-                    cudaEventRecord(e1, c->stream);
-                    c->launches += reps + 1;
-                    if (e != cudaSuccess) break;
-                    cudaEventSynchronize(e1);
-                    float ms = 0;
-                    cudaEventElapsedTime(&ms, e0, e1);
-                    if (ms < best_ms) {
-                        best_ms = ms;
-                        best = t;
-                    }
-                }
-    // the TMA bulk-staged kernels: three ring shapes, with and without PDL
-    for (int lp : {3, 4, 5})
-    for (int pdl : {0, 1}) {
-        if (e != cudaSuccess) break;
-        const bsg_tune t{1, 256, 0, lp, pdl};
-        const bsg::MapCfg cfg{1, 256, 0, lp, pdl};
+    // Times `reps` back-to-back passes (as the NUM_RUNS passes run) after one
+    // warm-up pass; a negative result: the launch failed or a bounded wait of
+    // the staged kernel expired (never pick such a shape).
+    auto time_cfg = [&](const bsg::MapCfg& cfg, int reps) -> float {
         e = bsg::launch_map(a, (int64_t)n, bsg::MODE_FAST, cfg, c->sm_count, c->stream);
-        if (e != cudaSuccess) break;
+        if (e != cudaSuccess) return -1.0f;
         cudaEventRecord(e0, c->stream);
         for (int i = 0; i < reps && e == cudaSuccess; ++i)
             e = bsg::launch_map(a, (int64_t)n, bsg::MODE_FAST, cfg, c->sm_count, c->stream);
         cudaEventRecord(e1, c->stream);
         c->launches += reps + 1;
-        if (e != cudaSuccess) break;
+        if (e != cudaSuccess) return -1.0f;
         cudaEventSynchronize(e1);
         float ms = 0;
         cudaEventElapsedTime(&ms, e0, e1);
-        if (bsg::bulk_error_take()) continue;  // never pick a shape whose wait expired
-        if (ms < best_ms) {
-            best_ms = ms;
-            best = t;
+        if (bsg::bulk_error_take()) return -1.0f;
+        return ms;
+    };
+    // sweep: every shape for 5 passes
+    std::vector<std::pair<float, bsg_tune>> timed;
+    for (int lp : {0, 1, 2, 6})
+        for (int vpt : {1, 2, 4})
+            for (int block : {128, 256, 512})
+                for (int bps : {0, 2, 4, 8})
+                for (int pdl : {0, 1}) {
+                    bsg_tune t{vpt, block, bps, lp, pdl};
+                    if (!tune_valid(&t) || e != cudaSuccess) continue;
+                    const float ms = time_cfg(bsg::MapCfg{vpt, block, bps, lp, pdl}, 5);
+                    if (ms >= 0) timed.push_back({ms, t});
+                }
+    // the TMA bulk-staged kernels: three ring shapes, with and without PDL
+    for (int lp : {3, 4, 5})
+        for (int pdl : {0, 1}) {
+            if (e != cudaSuccess) break;
+            const float ms = time_cfg(bsg::MapCfg{1, 256, 0, lp, pdl}, 5);
+            if (ms >= 0) timed.push_back({ms, bsg_tune{1, 256, 0, lp, pdl}});
         }
-    }
+    // final: the four fastest again over 25 passes each, twice, interleaved
+    // (longer runs show the steady state the L2 reaches across passes)
+    std::stable_sort(timed.begin(), timed.end(),
+                     [](const auto& x, const auto& y) { return x.first < y.first; });
+    if (timed.size() > 4) timed.resize(4);
+    std::vector<float> fin(timed.size(), 1e30f);
+    for (int round = 0; round < 2 && e == cudaSuccess; ++round)
+        for (size_t q = 0; q < timed.size() && e == cudaSuccess; ++q) {
+            const bsg_tune& t = timed[q].second;
+            const float ms = time_cfg(bsg::MapCfg{t.vec_per_thread, t.block, t.blocks_per_sm,
+                                                  t.load_path, t.pdl}, 25);
+            if (ms >= 0 && ms < fin[q]) fin[q] = ms;
+        }
+    float best_ms = 1e30f;
+    best = bsg_tune{1, 256, 0, 0, 0};
+    for (size_t q = 0; q < timed.size(); ++q)
+        if (fin[q] < best_ms) {
+            best_ms = fin[q];
+            best = timed[q].second;
+        }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (e != cudaSuccess) return cuda_fail(c, e, "autotune launch");

@@ -38,7 +38,8 @@ struct MapCfg {
     int block;         // threads per block
     int blocks_per_sm; // 0: one block per tile; else grid = blocks_per_sm * SMs
     int load_path;     // 0: v4 nc; 1: v4 + L2 evict_first; 2: v8 (256-bit) nc;
-                       // 3: TMA bulk copies into a shared-memory ring
+                       // 3, 4, 5: TMA bulk copies into a shared-memory ring;
+                       // 6: v8 + L2 evict_first
     int pdl;           // 1: launch with programmatic stream serialization
 };
 

@@ -28,8 +28,12 @@ struct Raw {
     uint32_t v[W];
 };
 
-// LP 0/2: ld.global.nc.L1::no_allocate (v4 / v8); LP 1: v4 plus an L2
-// evict_first cache policy.
+// Load paths of the vector kernel: LP 0/2: ld.global.nc.L1::no_allocate
+// (v4 / v8); LP 1 / 6: the same v4 / v8 loads with an L2 evict_first cache
+// policy.
+__host__ __device__ constexpr bool lp_evict_first(int lp) { return lp == 1 || lp == 6; }
+__host__ __device__ constexpr bool lp_v8(int lp) { return lp == 2 || lp == 6; }
+
 template <int W, int LP>
 __device__ __forceinline__ Raw<W> ld_group(const void* p, unsigned long long pol) {
     Raw<W> r;
@@ -44,6 +48,11 @@ __device__ __forceinline__ Raw<W> ld_group(const void* p, unsigned long long pol
                 : "=r"(r.v[0]), "=r"(r.v[1]), "=r"(r.v[2]), "=r"(r.v[3])
                 : "l"(p));
         }
+    } else if constexpr (lp_evict_first(LP)) {
+        asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
+            : "=r"(r.v[0]), "=r"(r.v[1]), "=r"(r.v[2]), "=r"(r.v[3]),
+              "=r"(r.v[4]), "=r"(r.v[5]), "=r"(r.v[6]), "=r"(r.v[7])
+            : "l"(p), "l"(pol));
     } else {
         (void)pol;
         asm("ld.global.nc.L1::no_allocate.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
@@ -103,10 +112,25 @@ __device__ __forceinline__ void price_groups(const SoA& a, int64_t g0, int64_t g
             if (g < g1) {
                 float p[W];
 #pragma unroll
-                for (int e = 0; e < W; ++e)
-                    p[e] = price<M>(__uint_as_float(S[j].v[e]), __uint_as_float(K[j].v[e]),
-                                    __uint_as_float(R[j].v[e]), __uint_as_float(V[j].v[e]),
-                                    __uint_as_float(T[j].v[e]), (int)O[j].v[e]);
+                for (int e = 0; e < W; e += 4) {
+                    const float4 q = price4<M>(
+                        make_float4(__uint_as_float(S[j].v[e]), __uint_as_float(S[j].v[e + 1]),
+                                    __uint_as_float(S[j].v[e + 2]), __uint_as_float(S[j].v[e + 3])),
+                        make_float4(__uint_as_float(K[j].v[e]), __uint_as_float(K[j].v[e + 1]),
+                                    __uint_as_float(K[j].v[e + 2]), __uint_as_float(K[j].v[e + 3])),
+                        make_float4(__uint_as_float(R[j].v[e]), __uint_as_float(R[j].v[e + 1]),
+                                    __uint_as_float(R[j].v[e + 2]), __uint_as_float(R[j].v[e + 3])),
+                        make_float4(__uint_as_float(V[j].v[e]), __uint_as_float(V[j].v[e + 1]),
+                                    __uint_as_float(V[j].v[e + 2]), __uint_as_float(V[j].v[e + 3])),
+                        make_float4(__uint_as_float(T[j].v[e]), __uint_as_float(T[j].v[e + 1]),
+                                    __uint_as_float(T[j].v[e + 2]), __uint_as_float(T[j].v[e + 3])),
+                        make_int4((int)O[j].v[e], (int)O[j].v[e + 1], (int)O[j].v[e + 2],
+                                  (int)O[j].v[e + 3]));
+                    p[e] = q.x;
+                    p[e + 1] = q.y;
+                    p[e + 2] = q.z;
+                    p[e + 3] = q.w;
+                }
                 st_group<W>(a.out + g * W, p);
             }
         }
@@ -130,9 +154,9 @@ __device__ __forceinline__ void pdl_wait() {
 }
 
 template <int M, int W, int VPT, int LP>
-__global__ void __launch_bounds__(512) map_vec_kernel(SoA a, int64_t n) {
+__global__ void __launch_bounds__(512, VPT == 1 ? 2 : 1) map_vec_kernel(SoA a, int64_t n) {
     pdl_trigger();
-    const unsigned long long pol = (LP == 1) ? evict_first_policy() : 0ull;
+    const unsigned long long pol = lp_evict_first(LP) ? evict_first_policy() : 0ull;
     const int64_t ngroups = n / W;
     const int64_t tile = (int64_t)blockDim.x * VPT;
     for (int64_t t0 = (int64_t)blockIdx.x * tile; t0 < ngroups; t0 += (int64_t)gridDim.x * tile) {
@@ -212,11 +236,15 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity,
 }
 
 // One 1D bulk copy of `bytes` (16-byte aligned at both ends, a multiple of
-// 16) into shared memory, completing on `bar`.
-__device__ __forceinline__ void bulk_copy(char* dst, const char* src, int bytes, uint32_t bar) {
+// 16) into shared memory, completing on `bar`, with L2 cache policy `pol`
+// (evict_first: the cyclic scan then keeps a slice of the inputs in L2 from
+// pass to pass, as the evict_first load paths do).
+__device__ __forceinline__ void bulk_copy(char* dst, const char* src, int bytes, uint32_t bar,
+                                          unsigned long long pol) {
     asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-        :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(bar) : "memory");
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+        " [%0], [%1], %2, [%3], %4;"
+        :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(bar), "l"(pol) : "memory");
 }
 
 // Issues the six copies of tile `tile` into stage memory `st` (thread 0).
@@ -229,12 +257,13 @@ __device__ __forceinline__ void bulk_issue(const SoA& a, int64_t tile, char* st,
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
                  :: "r"(bar), "r"(6 * TILE * 4 + tx_extra) : "memory");
     const size_t off = (size_t)tile * TILE * 4;
-    bulk_copy(st + 0 * TILE * 4, reinterpret_cast<const char*>(a.s) + off, TILE * 4, bar);
-    bulk_copy(st + 1 * TILE * 4, reinterpret_cast<const char*>(a.k) + off, TILE * 4, bar);
-    bulk_copy(st + 2 * TILE * 4, reinterpret_cast<const char*>(a.r) + off, TILE * 4, bar);
-    bulk_copy(st + 3 * TILE * 4, reinterpret_cast<const char*>(a.v) + off, TILE * 4, bar);
-    bulk_copy(st + 4 * TILE * 4, reinterpret_cast<const char*>(a.t) + off, TILE * 4, bar);
-    bulk_copy(st + 5 * TILE * 4, reinterpret_cast<const char*>(a.ot) + off, TILE * 4, bar);
+    const unsigned long long pol = evict_first_policy();
+    bulk_copy(st + 0 * TILE * 4, reinterpret_cast<const char*>(a.s) + off, TILE * 4, bar, pol);
+    bulk_copy(st + 1 * TILE * 4, reinterpret_cast<const char*>(a.k) + off, TILE * 4, bar, pol);
+    bulk_copy(st + 2 * TILE * 4, reinterpret_cast<const char*>(a.r) + off, TILE * 4, bar, pol);
+    bulk_copy(st + 3 * TILE * 4, reinterpret_cast<const char*>(a.v) + off, TILE * 4, bar, pol);
+    bulk_copy(st + 4 * TILE * 4, reinterpret_cast<const char*>(a.t) + off, TILE * 4, bar, pol);
+    bulk_copy(st + 5 * TILE * 4, reinterpret_cast<const char*>(a.ot) + off, TILE * 4, bar, pol);
 }
 
 template <int M, int OPT, int STAGES>
@@ -282,10 +311,11 @@ __global__ void __launch_bounds__(kBulkThreads) map_bulk_kernel(SoA a, int64_t n
             const float4 V = *reinterpret_cast<const float4*>(st + 3 * TILE * 4 + o);
             const float4 T = *reinterpret_cast<const float4*>(st + 4 * TILE * 4 + o);
             const int4 O = *reinterpret_cast<const int4*>(st + 5 * TILE * 4 + o);
-            p[h][0] = price<M>(S.x, K.x, R.x, V.x, T.x, O.x);
-            p[h][1] = price<M>(S.y, K.y, R.y, V.y, T.y, O.y);
-            p[h][2] = price<M>(S.z, K.z, R.z, V.z, T.z, O.z);
-            p[h][3] = price<M>(S.w, K.w, R.w, V.w, T.w, O.w);
+            const float4 q = price4<M>(S, K, R, V, T, O);
+            p[h][0] = q.x;
+            p[h][1] = q.y;
+            p[h][2] = q.z;
+            p[h][3] = q.w;
         }
         __syncthreads();  // every thread has read stage s
         if (threadIdx.x == 0 && k + STAGES < mine) {
@@ -329,6 +359,7 @@ static bool aligned(const void* p, uintptr_t al) {
 }
 
 bool map_vectorizable(const SoA& a, const MapCfg& cfg) {
+    // 256-bit loads for LP 2 and 6, and for the bulk paths' small-n fallback
     const uintptr_t al = (cfg.load_path >= 2) ? 32 : 16;
     return aligned(a.s, al) && aligned(a.k, al) && aligned(a.r, al) &&
            aligned(a.v, al) && aligned(a.t, al) && aligned(a.ot, al) &&
@@ -380,7 +411,7 @@ static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg,
         map_scalar_kernel<M><<<(unsigned)grid, 256, 0, st>>>(a, n);
         return cudaGetLastError();
     }
-    if (cfg.load_path >= 3) {
+    if (cfg.load_path >= 3 && cfg.load_path <= 5) {
         if constexpr (M == MODE_FAST) {
             // 3: <8 options, 3 stages>, 4: <4, 4>, 5: <4, 3>
             if (cfg.load_path == 3 && n >= BulkShape<8, 3>::tile)
@@ -395,7 +426,7 @@ static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg,
         v8.vpt = 1;
         return launch_map_mode<M>(a, n, v8, sm_count, st);
     }
-    const int W = (cfg.load_path == 2) ? 8 : 4;
+    const int W = lp_v8(cfg.load_path) ? 8 : 4;
     const int64_t ngroups = n / W;
     const int64_t tile = (int64_t)block * cfg.vpt;
     int64_t ntiles = (ngroups + tile - 1) / tile;
@@ -430,11 +461,13 @@ static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg,
             case 14: BSG_LAUNCH(4, 4, 1); break;
             case 21: BSG_LAUNCH(8, 1, 2); break;
             case 22: BSG_LAUNCH(8, 2, 2); break;
+            case 61: BSG_LAUNCH(8, 1, 6); break;
+            case 62: BSG_LAUNCH(8, 2, 6); break;
             default: return cudaErrorInvalidValue;
         }
     } else {
         // reference-order paths are validation variants: one shape.
-        if (cfg.load_path == 2) BSG_LAUNCH(8, 1, 2);
+        if (lp_v8(cfg.load_path)) BSG_LAUNCH(8, 1, 2);
         else BSG_LAUNCH(4, 1, 0);
     }
 #undef BSG_LAUNCH
@@ -499,7 +532,7 @@ cudaError_t launch_fp64(const SoA& a, double* out, int64_t n, int sm_count,
 // ------------------------------------------------------------ batched books
 // A tile is 8192 options; a block covers it in passes of kBatchBlock
 // threads x kBatchVpt v4 groups.
-constexpr int kBatchVpt = 2;
+constexpr int kBatchVpt = 1;
 constexpr uint64_t kBatchTileOptions = 8192;
 
 uint64_t batch_tile_options() { return kBatchTileOptions; }
@@ -528,7 +561,7 @@ __device__ __forceinline__ void price_range(const SoA& pool, uint64_t b, uint64_
 // prices it.  No block ever waits on another; the loop ends when the counter
 // passes the last tile.
 template <int M, int W>
-__global__ void __launch_bounds__(kBatchBlock) batch_kernel(
+__global__ void __launch_bounds__(kBatchBlock, 4) batch_kernel(
     SoA pool, const uint64_t* __restrict__ seg_off, const uint64_t* __restrict__ seg_len,
     const uint64_t* __restrict__ tile_prefix, int nseg, uint64_t ntiles, uint64_t topt,
     unsigned long long* cursor) {

@@ -171,12 +171,7 @@ __global__ void __launch_bounds__(kThreads) serve_fused_kernel(const Desc* __res
             const float4 V = reinterpret_cast<const float4*>(q.src[3])[g];
             const float4 T = reinterpret_cast<const float4*>(q.src[4])[g];
             const int4 O = reinterpret_cast<const int4*>(q.ot)[g];
-            float4 P;
-            P.x = bsg::price<M>(S.x, K.x, R.x, V.x, T.x, O.x);
-            P.y = bsg::price<M>(S.y, K.y, R.y, V.y, T.y, O.y);
-            P.z = bsg::price<M>(S.z, K.z, R.z, V.z, T.z, O.z);
-            P.w = bsg::price<M>(S.w, K.w, R.w, V.w, T.w, O.w);
-            reinterpret_cast<float4*>(q.out)[g] = P;
+            reinterpret_cast<float4*>(q.out)[g] = bsg::price4<M>(S, K, R, V, T, O);
         }
         for (uint64_t i = e4 + threadIdx.x; i < e; i += kThreads)
             q.out[i] = bsg::price<M>(q.src[0][i], q.src[1][i], q.src[2][i], q.src[3][i],

@@ -49,7 +49,8 @@ def test_guards_on_every_tune(debug_ctx):
     book = books.generate(CAP, seed=92)
     want = oracle.price_fp64(book)
     for tune in ((1, 256, 0, 0, 0), (2, 128, 2, 1, 1), (1, 256, 2, 2, 1),
-                 (1, 256, 0, 3, 1), (1, 256, 0, 4, 1), (1, 256, 0, 5, 0)):
+                 (1, 256, 0, 3, 1), (1, 256, 0, 4, 1), (1, 256, 0, 5, 0),
+                 (2, 128, 4, 6, 1)):
         debug_ctx.set_tune(*tune)
         for n in (CAP, 4099, 17):
             got = debug_ctx.price_book(book.slice(0, n), num_runs=2)

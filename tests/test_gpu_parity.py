@@ -125,7 +125,7 @@ def test_all_tunings_give_identical_bits(gpu_ctx):
     base = gpu_ctx.price_book(book)
     saved = gpu_ctx.get_tune()
     try:
-        for lp in (0, 1, 2, 3, 4, 5):
+        for lp in (0, 1, 2, 3, 4, 5, 6):
             for vpt in (1, 2, 4):
                 if lp >= 2 and vpt == 4:
                     continue
