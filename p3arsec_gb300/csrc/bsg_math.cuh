@@ -340,9 +340,11 @@ __device__ __forceinline__ float price_sfu_ref(float s, float k, float r, float 
 
 // float x double-literal product rounded to float, as the reference's
 // `float = float * <double literal>` lines evaluate (to within the rare
-// double-rounding case).
+// double-rounding case).  An infinite x gives c.hi * x, the double product's
+// value (c.hi x + c.lo x would be inf - inf when c.lo has the other sign).
 __device__ __forceinline__ float dmul(float x, FF c) {
-    return __fmaf_rn(c.hi, x, __fmul_rn(c.lo, x));
+    const float p = __fmaf_rn(c.hi, x, __fmul_rn(c.lo, x));
+    return isinf(x) ? __fmul_rn(c.hi, x) : p;
 }
 
 __device__ __forceinline__ float cndf_libm_ref(float x) {

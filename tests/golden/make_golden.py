@@ -51,6 +51,34 @@ def edge_book() -> books.Book:
                       a[:, 3].astype(f), a[:, 4].astype(f), a[:, 5].astype(np.int32))
 
 
+# Degenerate but finite inputs the reference prices without faulting:
+# expiry (t = 0), zero and extreme volatility, zero rate and price, tiny t,
+# a discount factor that underflows, S/K overflowing float, and negative t
+# or NaN inputs (the reference returns NaN).  Rows: S, K, r, v, t, otype.
+DEGENERATE = [
+    (100, 100, 0.05, 0.3, 0.0, 0), (100, 100, 0.05, 0.3, 0.0, 1),
+    (100, 90, 0.05, 0.3, 0.0, 0), (100, 110, 0.05, 0.3, 0.0, 1),
+    (90, 100, 0.05, 0.3, 0.0, 0), (110, 100, 0.05, 0.3, 0.0, 1),
+    (100, 100, 0.05, 0.0, 1.0, 0), (100, 90, 0.05, 0.0, 1.0, 0),
+    (100, 110, 0.05, 0.0, 1.0, 1), (100, 100, 0.0, 0.3, 1.0, 0),
+    (100, 100, 0.05, 0.3, -1.0, 0), (float("nan"), 100, 0.05, 0.3, 1, 0),
+    (100, 100, 0.05, float("nan"), 1, 1), (100, float("nan"), 0.05, 0.3, 1, 0),
+    (0.0, 100, 0.05, 0.3, 1, 0), (0.0, 100, 0.05, 0.3, 1, 1),
+    (100, 0.0, 0.05, 0.3, 1, 1), (100, 100, 0.05, 0.3, 1e-30, 0),
+    (100, 100, 0.05, 1e-20, 1.0, 0), (100, 100, 0.05, 50.0, 1.0, 0),
+    (100, 100, 0.05, 50.0, 1.0, 1), (100, 100, 5.0, 0.3, 100.0, 0),
+    (100, 100, 5.0, 0.3, 100.0, 1), (1e30, 1e-30, 0.05, 0.3, 1, 0),
+    (1e-30, 1e30, 0.05, 0.3, 1, 1),
+]
+
+
+def degenerate_book() -> books.Book:
+    a = np.array(DEGENERATE, dtype=np.float64)
+    f = np.float32
+    return books.Book(a[:, 0].astype(f), a[:, 1].astype(f), a[:, 2].astype(f),
+                      a[:, 3].astype(f), a[:, 4].astype(f), a[:, 5].astype(np.int32))
+
+
 CASES = {
     "plain_4096": lambda: books.generate(4096, seed=20240101, dist="plain"),
     "tails_4096": lambda: books.generate(4096, seed=20240102, dist="tails"),
@@ -112,6 +140,12 @@ def main():
         info["ref_vs_fp64_max_abs"] = float(np.max(np.abs(ref.astype(np.float64) - fp64)))
         meta[name] = info
         print(name, json.dumps(info))
+    # degenerate inputs: the compiled reference's prices only (no CLI run)
+    book = degenerate_book()
+    np.savez_compressed(os.path.join(HERE, "degenerate.npz"),
+                        sptprice=book.sptprice, strike=book.strike, rate=book.rate,
+                        volatility=book.volatility, otime=book.otime, otype=book.otype,
+                        ref_prices=oracle.price_reference(book))
     x = np.linspace(-8.0, 8.0, 4097, dtype=np.float32)
     x = np.concatenate([x, np.array([0.0, -0.0, 1e-8, -1e-8, 30.0, -30.0], dtype=np.float32)])
     R = oracle.ref_lib()

@@ -11,6 +11,8 @@ Tolerances (FP32 output):
     <= 5e-5 + 4 ulp of the price, most bit-identical.
   * FP64 kernel vs the CPU FP64 oracle: rtol 1e-12.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -279,3 +281,22 @@ def test_pipelined_host_calls_equal_synchronous_calls(gpu_ctx):
     assert np.array_equal(again.view(np.uint32), want[2].view(np.uint32))
     gpu_ctx.synchronize()
     assert np.array_equal(outs[0].view(np.uint32), want[0].view(np.uint32))
+
+
+@pytest.mark.parametrize("mode", ["fast", "sfu_ref", "libm_ref"])
+def test_degenerate_inputs_follow_the_reference(gpu_ctx, mode):
+    """Expiry (t = 0), zero and extreme volatility, zero prices, underflowing
+    discount, overflowing S/K, negative t and NaN inputs: NaN exactly where
+    the reference's own prices (tests/golden/degenerate.npz) are NaN, and the
+    finite prices within 1e-4 + 1e-6 |price|, at every vector-lane offset."""
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "degenerate.npz"))
+    book = books.Book(d["sptprice"], d["strike"], d["rate"], d["volatility"], d["otime"],
+                      d["otype"])
+    ref = d["ref_prices"].astype(np.float64)
+    for shift in range(8):
+        b = books.Book(*(np.roll(x, shift) for x in book.arrays()))
+        got = np.roll(gpu_ctx.price_book(b, mode=mode).astype(np.float64), -shift)
+        assert np.array_equal(np.isnan(got), np.isnan(ref)), (mode, shift, got, ref)
+        fin = ~np.isnan(ref)
+        tol = 1e-4 + 1e-6 * np.abs(ref[fin])
+        assert np.all(np.abs(got[fin] - ref[fin]) <= tol), (mode, shift, got[fin] - ref[fin])

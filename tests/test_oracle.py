@@ -124,3 +124,18 @@ def test_reference_simd_variants_agree_when_present(oracle_lib):
     assert np.array_equal(s2.view(np.uint64), oracle_lib.price_fp64(book).view(np.uint64))
     s4 = oracle_lib.price_reference_simd(book, 4)
     assert np.abs(s4.astype(np.float64) - s2).max() < 1e-3
+
+
+def test_restatement_on_degenerate_inputs(oracle_lib):
+    """Expiry, zero volatility, zero prices, overflow, negative t and NaN
+    inputs: the restatement gives the compiled reference's prices bit for
+    bit, NaN where it is NaN (tests/golden/degenerate.npz)."""
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "degenerate.npz"))
+    book = books.Book(d["sptprice"], d["strike"], d["rate"], d["volatility"], d["otime"],
+                      d["otype"])
+    got = oracle_lib.price_ref(book)
+    ref = d["ref_prices"]
+    assert np.array_equal(np.isnan(got), np.isnan(ref))
+    fin = ~np.isnan(ref)
+    assert np.array_equal(got[fin].view(np.uint32), ref[fin].view(np.uint32))
