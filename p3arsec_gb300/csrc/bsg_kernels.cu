@@ -1,10 +1,13 @@
 // bsg_kernels.cu -- sm_103a kernels of the Black-Scholes map.
 //
 // The hot path is an HBM-bound elementwise map: 28 bytes per option per run
-// (five float inputs, one int32 otype, one float price) against ~100 FP32/SFU
-// instructions.  Design:
+// (five float inputs, one int32 otype, one float price) against ~86 issued
+// instructions (the FAST arithmetic runs two options per packed f32x2
+// instruction).  Design:
 //  * SoA streams read with 128-bit (v4) or 256-bit (v8) non-coherent loads
-//    that do not allocate in L1; prices stored with streaming stores.
+//    that do not allocate in L1, optionally inserted into L2 as evict_first
+//    (a cyclic scan of a working set larger than L2 then keeps a slice of it
+//    resident between passes); prices stored with streaming stores.
 //  * Each thread loads VPT vector groups of all six arrays before computing,
 //    so a warp keeps 6 * VPT independent 512/1024-byte requests in flight.
 //  * Grid: one block per tile, or a persistent grid-stride loop sized in
@@ -146,6 +149,8 @@ __device__ __forceinline__ void price_groups(const SoA& a, int64_t g0, int64_t g
 // writes), and waits for the previous pass to complete only after its own
 // stores, so a pass still completes after the one before it.  Both
 // instructions are no-ops for a launch without the PDL attribute.
+// Registers: one-group shapes (VPT = 1) are held to 64 per thread (1024
+// threads per SM, no spills); more groups per thread need up to 128.
 __device__ __forceinline__ void pdl_trigger() {
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
