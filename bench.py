@@ -326,7 +326,12 @@ def run_batch(args, rank, world, local):
         ctx.autotune(1 << 16)  # plain per-book launches are small
     stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{local}")
     runs = args.runs
-    batch_tune = ctx.autotune_batch(dev, out_b, pool_len, segs)
+    if args.batch_tune:
+        tile, bps = (int(x) for x in args.batch_tune.split(","))
+        ctx.set_batch_tune(tile, bps)
+        batch_tune = ctx.get_batch_tune()
+    else:
+        batch_tune = ctx.autotune_batch(dev, out_b, pool_len, segs)
 
     def timed(fn):
         for _ in range(args.warmup):
@@ -705,6 +710,8 @@ def main(argv=None):
     ap.add_argument("--serve-fused", type=int, default=1,
                     help="1: one fused kernel per batch; 0: gather, price, scatter")
     ap.add_argument("--books", type=int, default=4096, help="batch config: number of books")
+    ap.add_argument("--batch-tune", default=None,
+                    help="batch config: tile_options,blocks_per_sm instead of autotuning")
     ap.add_argument("--n", type=int, default=N_OPTIONS)
     ap.add_argument("--runs", type=int, default=NUM_RUNS)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
