@@ -704,9 +704,10 @@ def main(argv=None):
                     default="map")
     ap.add_argument("--serve-rate", type=float, default=20000.0)
     ap.add_argument("--serve-rates",
-                    default="1000,5000,10000,15000,20000,30000,40000,50000,60000,70000,80000,90000")
+                    default="1000,2500,5000,7500,10000,15000,20000,30000,40000,45000,50000,"
+                            "55000,60000,70000,80000,90000")
     ap.add_argument("--serve-seconds", type=float, default=3.0)
-    ap.add_argument("--serve-inflight", type=int, default=4)
+    ap.add_argument("--serve-inflight", type=int, default=8)
     ap.add_argument("--serve-fused", type=int, default=1,
                     help="1: one fused kernel per batch; 0: gather, price, scatter")
     ap.add_argument("--books", type=int, default=4096, help="batch config: number of books")

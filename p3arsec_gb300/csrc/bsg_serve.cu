@@ -38,6 +38,10 @@
 #include <unordered_map>
 #include <vector>
 
+#ifdef __linux__
+#include <sys/prctl.h>
+#endif
+
 namespace {
 
 constexpr uint64_t kTile = 2048;   // options per ingest/egress/batch tile: small,
@@ -48,6 +52,15 @@ constexpr int kThreads = 256;
 double now_s() {
     using namespace std::chrono;
     return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+// The completer's timer slack is set to 1 us (a per-thread setting) so that
+// its short sleeps between event queries end on time instead of after the
+// default 50 us slack.
+void set_fine_timer_slack() {
+#ifdef __linux__
+    prctl(PR_SET_TIMERSLACK, 1000UL, 0UL, 0UL, 0UL);
+#endif
 }
 
 // One request of a batch as the ingest/egress kernels see it.  Host arrays
@@ -137,13 +150,15 @@ __global__ void __launch_bounds__(kThreads) egress_kernel(const Desc* __restrict
 // output.  Tiles come from a per-slot counter that only grows: this launch's
 // tiles are [base, base + ntiles) of it, and every block ends with exactly
 // one failing increment, so the next launch's base is base + ntiles + grid
-// (no reset between batches).
+// (no reset between batches).  A thread issues the loads of both of its
+// 4-option groups of a full tile before pricing either, so each block keeps
+// 12 host-memory requests per thread in flight across the link.
 template <int M>
-__global__ void __launch_bounds__(kThreads) serve_fused_kernel(const Desc* __restrict__ d,
-                                                               const uint64_t* __restrict__ pre,
-                                                               int m, uint64_t ntiles,
-                                                               unsigned long long* counter,
-                                                               unsigned long long base) {
+__device__ __forceinline__ void fused_tiles(const Desc* __restrict__ d,
+                                            const uint64_t* __restrict__ pre, int m,
+                                            uint64_t ntiles, unsigned long long* counter,
+                                            unsigned long long base) {
+    static_assert(kTile == 8 * kThreads, "two 4-option groups per thread per tile");
     __shared__ int sh_q, sh_done;
     __shared__ uint64_t sh_tile;
     for (;;) {
@@ -164,6 +179,24 @@ __global__ void __launch_bounds__(kThreads) serve_fused_kernel(const Desc* __res
         const uint64_t b = (tile - pre[qi]) * kTile;
         const uint64_t e = (b + kTile < q.n) ? b + kTile : q.n;
         const uint64_t e4 = q.vec ? b + ((e - b) & ~3ull) : b;
+        if (e4 - b == kTile) {  // a full vector tile: both groups' loads first
+            const uint64_t g0 = b / 4 + threadIdx.x, g1 = g0 + kThreads;
+            const float4 S0 = reinterpret_cast<const float4*>(q.src[0])[g0];
+            const float4 K0 = reinterpret_cast<const float4*>(q.src[1])[g0];
+            const float4 R0 = reinterpret_cast<const float4*>(q.src[2])[g0];
+            const float4 V0 = reinterpret_cast<const float4*>(q.src[3])[g0];
+            const float4 T0 = reinterpret_cast<const float4*>(q.src[4])[g0];
+            const int4 O0 = reinterpret_cast<const int4*>(q.ot)[g0];
+            const float4 S1 = reinterpret_cast<const float4*>(q.src[0])[g1];
+            const float4 K1 = reinterpret_cast<const float4*>(q.src[1])[g1];
+            const float4 R1 = reinterpret_cast<const float4*>(q.src[2])[g1];
+            const float4 V1 = reinterpret_cast<const float4*>(q.src[3])[g1];
+            const float4 T1 = reinterpret_cast<const float4*>(q.src[4])[g1];
+            const int4 O1 = reinterpret_cast<const int4*>(q.ot)[g1];
+            reinterpret_cast<float4*>(q.out)[g0] = bsg::price4<M>(S0, K0, R0, V0, T0, O0);
+            reinterpret_cast<float4*>(q.out)[g1] = bsg::price4<M>(S1, K1, R1, V1, T1, O1);
+            continue;
+        }
         for (uint64_t g = b / 4 + threadIdx.x; g < e4 / 4; g += kThreads) {
             const float4 S = reinterpret_cast<const float4*>(q.src[0])[g];
             const float4 K = reinterpret_cast<const float4*>(q.src[1])[g];
@@ -179,6 +212,32 @@ __global__ void __launch_bounds__(kThreads) serve_fused_kernel(const Desc* __res
     }
 }
 
+// Table in device memory (copied there before the launch).
+template <int M>
+__global__ void __launch_bounds__(kThreads) serve_fused_kernel(const Desc* __restrict__ d,
+                                                               const uint64_t* __restrict__ pre,
+                                                               int m, uint64_t ntiles,
+                                                               unsigned long long* counter,
+                                                               unsigned long long base) {
+    fused_tiles<M>(d, pre, m, ntiles, counter, base);
+}
+
+// Batches of up to kInline requests carry their table in the kernel's
+// parameters (__grid_constant__: read in place, no copy before the launch).
+constexpr int kInline = 24;
+struct InlineTable {
+    Desc d[kInline];
+    uint64_t pre[kInline + 1];
+};
+static_assert(sizeof(InlineTable) <= 4000, "kernel parameter space");
+
+template <int M>
+__global__ void __launch_bounds__(kThreads) serve_fused_inline_kernel(
+    const __grid_constant__ InlineTable tab, int m, uint64_t ntiles,
+    unsigned long long* counter, unsigned long long base) {
+    fused_tiles<M>(tab.d, tab.pre, m, ntiles, counter, base);
+}
+
 cudaError_t launch_fused(int mode, unsigned grid, cudaStream_t st, const Desc* d,
                          const uint64_t* pre, int m, uint64_t ntiles,
                          unsigned long long* counter, unsigned long long base) {
@@ -191,6 +250,23 @@ cudaError_t launch_fused(int mode, unsigned grid, cudaStream_t st, const Desc* d
             break;
         default:
             serve_fused_kernel<bsg::MODE_LIBM_REF><<<grid, kThreads, 0, st>>>(d, pre, m, ntiles, counter, base);
+            break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fused_inline(int mode, unsigned grid, cudaStream_t st, const InlineTable& tab,
+                                int m, uint64_t ntiles, unsigned long long* counter,
+                                unsigned long long base) {
+    switch (mode) {
+        case bsg::MODE_FAST:
+            serve_fused_inline_kernel<bsg::MODE_FAST><<<grid, kThreads, 0, st>>>(tab, m, ntiles, counter, base);
+            break;
+        case bsg::MODE_SFU_REF:
+            serve_fused_inline_kernel<bsg::MODE_SFU_REF><<<grid, kThreads, 0, st>>>(tab, m, ntiles, counter, base);
+            break;
+        default:
+            serve_fused_inline_kernel<bsg::MODE_LIBM_REF><<<grid, kThreads, 0, st>>>(tab, m, ntiles, counter, base);
             break;
     }
     return cudaGetLastError();
@@ -344,6 +420,22 @@ struct bsg_server {
         }
         hpre[m] = acc;
         const uint64_t ntiles = acc;
+        const unsigned grid = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)sm_count * 8);
+        if (cfg.fused && m <= kInline) {
+            // the table travels in the launch's parameters: no copy
+            InlineTable tab;
+            for (int i = 0; i < m; ++i) {
+                tab.d[i] = hd[i];
+                tab.pre[i] = hpre[i];
+            }
+            tab.pre[m] = hpre[m];
+            unsigned long long* ctr = sl.d_cursor + 1;
+            if (launch_fused_inline(mode, grid, sl.st, tab, m, ntiles, ctr, sl.fused_base) != cudaSuccess)
+                return BSG_ERR_CUDA;
+            sl.fused_base += ntiles + grid;
+            if (cudaEventRecord(sl.ev, sl.st) != cudaSuccess) return BSG_ERR_CUDA;
+            return BSG_OK;
+        }
         const size_t bytes = (size_t)m * sizeof(Desc) + (3 * (size_t)m + 1) * sizeof(uint64_t);
         if (cudaMemcpyAsync(sl.d_tab, sl.h_tab, bytes, cudaMemcpyHostToDevice, sl.st) != cudaSuccess)
             return BSG_ERR_CUDA;
@@ -351,7 +443,6 @@ struct bsg_server {
         const uint64_t* doff = reinterpret_cast<const uint64_t*>(sl.d_tab + (size_t)m * sizeof(Desc));
         const uint64_t* dlen = doff + m;
         const uint64_t* dpre = dlen + m;
-        const unsigned grid = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)sm_count * 8);
         if (cfg.fused) {
             // counter lives after the batch kernel's cursor word
             unsigned long long* ctr = sl.d_cursor + 1;
@@ -482,7 +573,8 @@ struct bsg_server {
         }
     }
 
-    // Bounded wait for one batch: cudaEventQuery with short sleeps.
+    // Bounded wait for one batch: cudaEventQuery, a few back to back, then
+    // with 5 us sleeps (fine timer slack: see set_fine_timer_slack).
     int wait_event(cudaEvent_t ev) {
         const double t_end = now_s() + batch_timeout;
         int spins = 0;
@@ -494,13 +586,14 @@ struct bsg_server {
                 return BSG_ERR_CUDA;
             }
             if (now_s() > t_end) return BSG_ERR_TIMEOUT;
-            if (++spins > 64) std::this_thread::sleep_for(std::chrono::microseconds(10));
+            if (++spins > 16) std::this_thread::sleep_for(std::chrono::microseconds(5));
         }
     }
 
     // -------------------------------------------------------- completer
     void completer() {
         cudaSetDevice(device);
+        set_fine_timer_slack();
         std::unique_lock<std::mutex> lk(mu);
         for (;;) {
             cv_comp.wait(lk, [&] { return stop || !inflight.empty(); });

@@ -69,7 +69,9 @@ def test_each_result_same_alone_and_in_mix(gpu_ctx, fused):
         stats = srv.stats()
         assert stats["completed"] == len(reqs)
         assert stats["batches"] < len(reqs) / 4  # requests were coalesced
-        assert stats["max_batch_requests_seen"] > 10
+        # batches of more than 24 requests take the copied-table launch, the
+        # single requests below the table-in-parameters launch
+        assert stats["max_batch_requests_seen"] > 24
         # alone: one request in flight at a time
         for o, n in reqs[:50]:
             st, _ = srv.wait(srv.submit(*[a[o:] for a in host], alone[o:], n=n), timeout_s=60.0)
