@@ -477,11 +477,12 @@ def run_serve(args, rank, world, local):
     host = [torch.from_numpy(a).pin_memory().numpy() for a in book.arrays()]
     out = torch.zeros(pool_n, dtype=torch.float32).pin_memory().numpy()
     rates = [float(x) for x in args.serve_rates.split(",")]
+    lo_n, hi_n = (int(x) for x in args.serve_sizes.split(","))
     sweep = {"batched": [], "plain": []}
     for mode in ("batched", "plain"):
         for rate in rates:
             res = abi.serve_trace(host, out, rate_per_s=rate, duration_s=args.serve_seconds,
-                                  min_n=16, max_n=1 << 20, seed=SEED + int(rate),
+                                  min_n=lo_n, max_n=hi_n, seed=SEED + int(rate),
                                   device=local, budget_bytes=64 << 30,
                                   max_inflight=args.serve_inflight,
                                   plain=(mode == "plain"), drain_timeout_s=60.0,
@@ -514,7 +515,7 @@ def run_serve(args, rank, world, local):
         "value": a["options_per_s"], "unit": UNIT, "n_gpus": world,
         "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded trace and books)",
         "config": {"workload": f"open-loop Poisson trace at {args.serve_rate:g} req/s for "
-                               f"{args.serve_seconds:g} s, sizes log-uniform in [16, 2^20], "
+                               f"{args.serve_seconds:g} s, sizes log-uniform in [{lo_n}, {hi_n}], "
                                f"64 GB device budget, {args.serve_inflight} batches in flight",
                    "fused": bool(args.serve_fused),
                    "rates_swept": rates, "seconds_per_point": args.serve_seconds},
@@ -707,6 +708,8 @@ def main(argv=None):
                     default="1000,2500,5000,7500,10000,15000,20000,30000,40000,45000,50000,"
                             "55000,60000,70000,80000,90000")
     ap.add_argument("--serve-seconds", type=float, default=3.0)
+    ap.add_argument("--serve-sizes", default="16,1048576",
+                    help="serve config: request sizes log-uniform in [lo, hi] options")
     ap.add_argument("--serve-inflight", type=int, default=8)
     ap.add_argument("--serve-fused", type=int, default=1,
                     help="1: one fused kernel per batch; 0: gather, price, scatter")
