@@ -486,7 +486,8 @@ def run_serve(args, rank, world, local):
                                   device=local, budget_bytes=64 << 30,
                                   max_inflight=args.serve_inflight,
                                   plain=(mode == "plain"), drain_timeout_s=60.0,
-                                  fused=(mode == "batched" and args.serve_fused))
+                                  fused=(mode == "batched" and args.serve_fused >= 1),
+                                  persistent=(mode == "batched" and args.serve_fused == 2))
             res["rate_per_s"] = rate
             sweep[mode].append(res)
             print(json.dumps({"serve_point": mode, **res}), file=sys.stderr, flush=True)
@@ -517,7 +518,10 @@ def run_serve(args, rank, world, local):
         "config": {"workload": f"open-loop Poisson trace at {args.serve_rate:g} req/s for "
                                f"{args.serve_seconds:g} s, sizes log-uniform in [{lo_n}, {hi_n}], "
                                f"64 GB device budget, {args.serve_inflight} batches in flight",
-                   "fused": bool(args.serve_fused),
+                   "batched_path": {0: "gather, batch kernel, scatter",
+                                    1: "one fused kernel per batch",
+                                    2: "persistent kernel over a host-memory request ring"}
+                                   [args.serve_fused],
                    "rates_swept": rates, "seconds_per_point": args.serve_seconds},
         "latency_s": {"p50": a["p50_s"], "p99": a["p99_s"], "p999": a["p999_s"], "max": a["max_s"]},
         "plain_at_rate": {k: at["plain"][k] for k in ("options_per_s", "p50_s", "p99_s", "p999_s",
@@ -711,8 +715,9 @@ def main(argv=None):
     ap.add_argument("--serve-sizes", default="16,1048576",
                     help="serve config: request sizes log-uniform in [lo, hi] options")
     ap.add_argument("--serve-inflight", type=int, default=8)
-    ap.add_argument("--serve-fused", type=int, default=1,
-                    help="1: one fused kernel per batch; 0: gather, price, scatter")
+    ap.add_argument("--serve-fused", type=int, default=2,
+                    help="2: the persistent kernel; 1: one fused kernel per batch; "
+                         "0: gather, price, scatter")
     ap.add_argument("--books", type=int, default=4096, help="batch config: number of books")
     ap.add_argument("--batch-tune", default=None,
                     help="batch config: tile_options,blocks_per_sm instead of autotuning")

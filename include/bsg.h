@@ -231,6 +231,12 @@ int bsg_error_report(bsg_ctx* ctx, const float* sptprice, const float* strike,
  * persistent batch kernel prices them, one kernel writes the prices back to
  * each request's host output.  Up to max_inflight batches overlap on the
  * GPU (one stream each).  With fused = 1 the three steps are one kernel.
+ * With fused = 2 one persistent kernel keeps running instead: each admitted
+ * request is published into a ring in pinned host memory that the GPU's
+ * blocks take tiles from (no launch, copy or event per request); the kernel
+ * exits after 5 ms without work and is relaunched when work arrives.  It
+ * needs host-native atomics (NVLink-C2C; else BSG_ERR_NOT_SUPPORTED) and
+ * takes requests of up to 4095 x 2048 options (else BSG_ERR_CAPACITY).
  * With plain = 1 the loop instead prices one request
  * at a time with per-array copies and one plain map launch (the baseline).
  * Request arrays are host memory; pinned memory (bsg_host_alloc or
@@ -250,6 +256,7 @@ typedef struct bsg_server_config {
     int fused;                /* 1 = one kernel per batch reads the inputs from
                                  host memory, prices them and writes the prices
                                  back (the pool then only accounts the budget);
+                                 2 = the persistent kernel (no device pool);
                                  0 = gather into the pool, price, scatter */
 } bsg_server_config;
 

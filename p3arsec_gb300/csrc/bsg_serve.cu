@@ -145,20 +145,58 @@ __global__ void __launch_bounds__(kThreads) egress_kernel(const Desc* __restrict
     }
 }
 
+// Prices options [b, min(b + kTile, n)) of request q: inputs read from the
+// request's (host) arrays, prices written to its (host) output.  A thread
+// issues the loads of both of its 4-option groups of a full tile before
+// pricing either, so a block keeps 12 requests per thread in flight.
+template <int M>
+__device__ __forceinline__ void price_request_tile(const Desc& q, uint64_t b) {
+    static_assert(kTile == 8 * kThreads, "two 4-option groups per thread per tile");
+    const uint64_t e = (b + kTile < q.n) ? b + kTile : q.n;
+    const uint64_t e4 = q.vec ? b + ((e - b) & ~3ull) : b;
+    if (e4 - b == kTile) {  // a full vector tile: both groups' loads first
+        const uint64_t g0 = b / 4 + threadIdx.x, g1 = g0 + kThreads;
+        const float4 S0 = reinterpret_cast<const float4*>(q.src[0])[g0];
+        const float4 K0 = reinterpret_cast<const float4*>(q.src[1])[g0];
+        const float4 R0 = reinterpret_cast<const float4*>(q.src[2])[g0];
+        const float4 V0 = reinterpret_cast<const float4*>(q.src[3])[g0];
+        const float4 T0 = reinterpret_cast<const float4*>(q.src[4])[g0];
+        const int4 O0 = reinterpret_cast<const int4*>(q.ot)[g0];
+        const float4 S1 = reinterpret_cast<const float4*>(q.src[0])[g1];
+        const float4 K1 = reinterpret_cast<const float4*>(q.src[1])[g1];
+        const float4 R1 = reinterpret_cast<const float4*>(q.src[2])[g1];
+        const float4 V1 = reinterpret_cast<const float4*>(q.src[3])[g1];
+        const float4 T1 = reinterpret_cast<const float4*>(q.src[4])[g1];
+        const int4 O1 = reinterpret_cast<const int4*>(q.ot)[g1];
+        reinterpret_cast<float4*>(q.out)[g0] = bsg::price4<M>(S0, K0, R0, V0, T0, O0);
+        reinterpret_cast<float4*>(q.out)[g1] = bsg::price4<M>(S1, K1, R1, V1, T1, O1);
+        return;
+    }
+    for (uint64_t g = b / 4 + threadIdx.x; g < e4 / 4; g += kThreads) {
+        const float4 S = reinterpret_cast<const float4*>(q.src[0])[g];
+        const float4 K = reinterpret_cast<const float4*>(q.src[1])[g];
+        const float4 R = reinterpret_cast<const float4*>(q.src[2])[g];
+        const float4 V = reinterpret_cast<const float4*>(q.src[3])[g];
+        const float4 T = reinterpret_cast<const float4*>(q.src[4])[g];
+        const int4 O = reinterpret_cast<const int4*>(q.ot)[g];
+        reinterpret_cast<float4*>(q.out)[g] = bsg::price4<M>(S, K, R, V, T, O);
+    }
+    for (uint64_t i = e4 + threadIdx.x; i < e; i += kThreads)
+        q.out[i] = bsg::price<M>(q.src[0][i], q.src[1][i], q.src[2][i], q.src[3][i],
+                                 q.src[4][i], q.ot[i]);
+}
+
 // Fused path: one kernel per batch reads each request's inputs from host
 // memory, prices them and writes the prices back to the request's host
 // output.  Tiles come from a per-slot counter that only grows: this launch's
 // tiles are [base, base + ntiles) of it, and every block ends with exactly
 // one failing increment, so the next launch's base is base + ntiles + grid
-// (no reset between batches).  A thread issues the loads of both of its
-// 4-option groups of a full tile before pricing either, so each block keeps
-// 12 host-memory requests per thread in flight across the link.
+// (no reset between batches).
 template <int M>
 __device__ __forceinline__ void fused_tiles(const Desc* __restrict__ d,
                                             const uint64_t* __restrict__ pre, int m,
                                             uint64_t ntiles, unsigned long long* counter,
                                             unsigned long long base) {
-    static_assert(kTile == 8 * kThreads, "two 4-option groups per thread per tile");
     __shared__ int sh_q, sh_done;
     __shared__ uint64_t sh_tile;
     for (;;) {
@@ -175,40 +213,7 @@ __device__ __forceinline__ void fused_tiles(const Desc* __restrict__ d,
         const int qi = sh_q;
         const uint64_t tile = sh_tile;
         __syncthreads();
-        const Desc q = d[qi];
-        const uint64_t b = (tile - pre[qi]) * kTile;
-        const uint64_t e = (b + kTile < q.n) ? b + kTile : q.n;
-        const uint64_t e4 = q.vec ? b + ((e - b) & ~3ull) : b;
-        if (e4 - b == kTile) {  // a full vector tile: both groups' loads first
-            const uint64_t g0 = b / 4 + threadIdx.x, g1 = g0 + kThreads;
-            const float4 S0 = reinterpret_cast<const float4*>(q.src[0])[g0];
-            const float4 K0 = reinterpret_cast<const float4*>(q.src[1])[g0];
-            const float4 R0 = reinterpret_cast<const float4*>(q.src[2])[g0];
-            const float4 V0 = reinterpret_cast<const float4*>(q.src[3])[g0];
-            const float4 T0 = reinterpret_cast<const float4*>(q.src[4])[g0];
-            const int4 O0 = reinterpret_cast<const int4*>(q.ot)[g0];
-            const float4 S1 = reinterpret_cast<const float4*>(q.src[0])[g1];
-            const float4 K1 = reinterpret_cast<const float4*>(q.src[1])[g1];
-            const float4 R1 = reinterpret_cast<const float4*>(q.src[2])[g1];
-            const float4 V1 = reinterpret_cast<const float4*>(q.src[3])[g1];
-            const float4 T1 = reinterpret_cast<const float4*>(q.src[4])[g1];
-            const int4 O1 = reinterpret_cast<const int4*>(q.ot)[g1];
-            reinterpret_cast<float4*>(q.out)[g0] = bsg::price4<M>(S0, K0, R0, V0, T0, O0);
-            reinterpret_cast<float4*>(q.out)[g1] = bsg::price4<M>(S1, K1, R1, V1, T1, O1);
-            continue;
-        }
-        for (uint64_t g = b / 4 + threadIdx.x; g < e4 / 4; g += kThreads) {
-            const float4 S = reinterpret_cast<const float4*>(q.src[0])[g];
-            const float4 K = reinterpret_cast<const float4*>(q.src[1])[g];
-            const float4 R = reinterpret_cast<const float4*>(q.src[2])[g];
-            const float4 V = reinterpret_cast<const float4*>(q.src[3])[g];
-            const float4 T = reinterpret_cast<const float4*>(q.src[4])[g];
-            const int4 O = reinterpret_cast<const int4*>(q.ot)[g];
-            reinterpret_cast<float4*>(q.out)[g] = bsg::price4<M>(S, K, R, V, T, O);
-        }
-        for (uint64_t i = e4 + threadIdx.x; i < e; i += kThreads)
-            q.out[i] = bsg::price<M>(q.src[0][i], q.src[1][i], q.src[2][i], q.src[3][i],
-                                     q.src[4][i], q.ot[i]);
+        price_request_tile<M>(d[qi], (tile - pre[qi]) * kTile);
     }
 }
 
@@ -272,6 +277,172 @@ cudaError_t launch_fused_inline(int mode, unsigned grid, cudaStream_t st, const 
     return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Persistent path: one kernel keeps running while requests arrive.  The host
+// writes each request into a ring of entries in pinned host memory (read by
+// the GPU over NVLink-C2C) and raises `published`; the blocks take tiles of
+// the oldest request with unclaimed tiles, price them, and the block that
+// finishes a request's last tile sets the entry's completion flag, which the
+// host polls.  No launch, table copy or event per request.
+//
+// Tile claims and done counts live in device memory (GPU-scope atomics; one
+// word of each per ring slot, reused lap after lap).  Claim word = tag (low 32
+// bits of the request's sequence number) << 32 | ntiles << 20 | tiles
+// claimed.  A block that sees its request's tag claims with one add and
+// decodes the value it replaced (count < ntiles: a tile); a slot still
+// tagged with the previous lap is re-armed for the request with a CAS, its
+// tile count read from the published entry; a slot tagged with a later lap
+// means the request is finished.  The only wait is a block finding no
+// published work: bounded by idle_ns of GPU time (and the host's stop
+// flag), after which the block exits; the host relaunches the kernel when
+// work arrives and no kernel is running.
+constexpr uint32_t kMaxRequestTiles = 4095;  // 12 bits of the claim word
+
+struct alignas(128) PEntry {
+    unsigned long long flag;    // seq + 1 once every tile is priced (GPU writes)
+    unsigned long long seq;     // request sequence number
+    unsigned long long ntiles;
+    Desc d;
+};
+
+struct alignas(64) PCtl {
+    unsigned long long published;   // requests 0 .. published-1 are in the ring
+    unsigned long long pad[7];
+    unsigned int stop;              // 1: blocks exit at their next idle check
+};
+
+__device__ __forceinline__ unsigned long long ld_acquire_sys(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned ld_relaxed_sys_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.relaxed.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_gpu(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned atom_add_acq_rel_gpu(unsigned* p, unsigned v) {
+    unsigned old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+    return old;
+}
+__device__ __forceinline__ void st_release_sys(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.release.sys.global.u64 [%0], %1;" :: "l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+template <int M>
+__global__ void __launch_bounds__(kThreads) serve_persistent_kernel(
+    PEntry* ring, unsigned long long rmask, const PCtl* ctl, unsigned long long* cur,
+    unsigned long long* taken, unsigned* done, unsigned long long idle_ns) {
+    __shared__ Desc sh_d;
+    __shared__ unsigned long long sh_b, sh_seq, sh_nt;
+    __shared__ int sh_ok;
+    // thread 0's view of `published` (re-read from host memory only when the
+    // ring looks drained) and the request whose descriptor sh_d holds
+    unsigned long long pub = 0, d_seq = ~0ull;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            sh_ok = 0;
+            unsigned backoff = 64;
+            unsigned long long t0 = global_ns();
+            while (ld_relaxed_sys_u32(&ctl->stop) == 0) {
+                const unsigned long long r = ld_relaxed_gpu(cur);
+                if (r >= pub) pub = ld_acquire_sys(&ctl->published);
+                if (r >= pub) {  // nothing published
+                    if (global_ns() - t0 > idle_ns) break;  // bounded idle wait
+                    __nanosleep(backoff);
+                    if (backoff < 8192) backoff *= 2;
+                    continue;
+                }
+                const unsigned long long slot = r & rmask;
+                const unsigned tag = (unsigned)r;
+                unsigned long long w = ld_relaxed_gpu(taken + slot);
+                bool advance = false;
+                for (;;) {
+                    const int lap = (int)((unsigned)(w >> 32) - tag);
+                    if (lap < 0) {  // slot still armed for the previous lap: arm it for r
+                        const unsigned long long nt = ring[slot].ntiles;  // published entry r
+                        const unsigned long long want = (unsigned long long)tag << 32 | nt << 20;
+                        const unsigned long long seen = atomicCAS(taken + slot, w, want);
+                        w = (seen == w) ? want : seen;
+                        continue;
+                    }
+                    if (lap > 0) {  // a later lap: request r is finished
+                        advance = true;
+                        break;
+                    }
+                    const unsigned long long old = atomicAdd(taken + slot, 1ull);
+                    if ((unsigned)(old >> 32) != tag) {  // re-armed meanwhile
+                        w = old;
+                        continue;
+                    }
+                    const unsigned long long c = old & 0xFFFFFull, nt = (old >> 20) & 0xFFFull;
+                    if (c < nt) {  // tile c of request r
+                        if (d_seq != r) {  // consecutive tiles of one request: read once
+                            sh_d = ring[slot].d;
+                            d_seq = r;
+                        }
+                        sh_b = c * kTile;
+                        sh_seq = r;
+                        sh_nt = nt;
+                        sh_ok = 1;
+                    } else {
+                        advance = true;  // every tile of r is claimed
+                    }
+                    break;
+                }
+                if (sh_ok) break;
+                if (advance) atomicCAS(cur, r, r + 1);
+                t0 = global_ns();
+                backoff = 64;
+            }
+        }
+        __syncthreads();
+        if (!sh_ok) break;
+        const Desc q = sh_d;
+        price_request_tile<M>(q, sh_b);
+        __threadfence_system();  // this thread's prices reach host memory first
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const unsigned long long slot = sh_seq & rmask;
+            if (atom_add_acq_rel_gpu(done + slot, 1u) + 1u == (unsigned)sh_nt) {
+                // the request's last tile: every block's prices are in host
+                // memory (each fenced before its count); re-arm the count
+                done[slot] = 0u;
+                st_release_sys(&ring[slot].flag, sh_seq + 1ull);
+            }
+        }
+    }
+}
+
+cudaError_t launch_persistent(int mode, unsigned grid, cudaStream_t st, PEntry* ring,
+                              unsigned long long rmask, const PCtl* ctl, unsigned long long* cur,
+                              unsigned long long* taken, unsigned* done,
+                              unsigned long long idle_ns) {
+    switch (mode) {
+        case bsg::MODE_FAST:
+            serve_persistent_kernel<bsg::MODE_FAST><<<grid, kThreads, 0, st>>>(ring, rmask, ctl, cur, taken, done, idle_ns);
+            break;
+        case bsg::MODE_SFU_REF:
+            serve_persistent_kernel<bsg::MODE_SFU_REF><<<grid, kThreads, 0, st>>>(ring, rmask, ctl, cur, taken, done, idle_ns);
+            break;
+        default:
+            serve_persistent_kernel<bsg::MODE_LIBM_REF><<<grid, kThreads, 0, st>>>(ring, rmask, ctl, cur, taken, done, idle_ns);
+            break;
+    }
+    return cudaGetLastError();
+}
+
 enum State { Q_QUEUED, Q_ADMITTED, Q_DONE };
 
 struct Request {
@@ -286,6 +457,8 @@ struct Request {
     bool auto_release;
     double* lat_slot;
     Desc desc;
+    uint64_t seq = 0, ntiles = 0;  // persistent path: ring sequence number, tiles
+    double t_pub = 0;              // persistent path: publication time
 };
 
 struct Slot {
@@ -338,11 +511,28 @@ size_t table_bytes(int cap) {
 
 }  // namespace
 
+constexpr uint64_t kRing = 4096;                 // persistent ring entries
+constexpr unsigned long long kIdleNs = 5000000;  // a block's idle bound: 5 ms
+
 struct bsg_server {
     bsg_server_config cfg{};
     int device = 0, sm_count = 0, batch_grid = 1, mode = 0, max_req = 4096;
     double batch_timeout = 30.0;
     char* d_pool = nullptr;
+    // persistent path (cfg.fused == 2)
+    bool persistent = false, broken = false;
+    PEntry* ring_h = nullptr;   // pinned host ring, and the GPU's address of it
+    PEntry* ring_d = nullptr;
+    PCtl* ctl_h = nullptr;
+    PCtl* ctl_d = nullptr;
+    unsigned long long* d_cur = nullptr;  // oldest request that may have unclaimed tiles
+    unsigned long long* d_taken = nullptr;  // per ring slot: claim word
+    unsigned* d_done = nullptr;             // per ring slot: tiles priced
+    cudaStream_t pst = nullptr;
+    cudaEvent_t pev = nullptr;            // recorded after each launch of the kernel
+    unsigned pgrid = 1;
+    uint64_t next_seq = 0;
+    std::deque<Request*> pinflight;       // published, not complete, in sequence order
     uint64_t cap = 0;  // options
     bsg::SoA pool{};
     std::map<uint64_t, uint64_t> free_list;  // start -> length (options)
@@ -513,9 +703,148 @@ struct bsg_server {
         }
     }
 
+    // ------------------------------------------------- persistent path
+    // Launches the persistent kernel unless one is running.  Only the
+    // completer thread calls it, without holding mu, so that a slow driver
+    // call never blocks submitting threads.
+    int ensure_kernel(bool* launched) {
+        *launched = false;
+        const cudaError_t q = cudaEventQuery(pev);
+        if (q == cudaErrorNotReady) return BSG_OK;
+        if (q != cudaSuccess) {
+            cudaGetLastError();
+            return BSG_ERR_CUDA;
+        }
+        // callers include submitting threads: launch on the server's device
+        int prev = device;
+        cudaGetDevice(&prev);
+        if (prev != device) cudaSetDevice(device);
+        const bool ok = launch_persistent(mode, pgrid, pst, ring_d, kRing - 1, ctl_d, d_cur,
+                                          d_taken, d_done, kIdleNs) == cudaSuccess &&
+                        cudaEventRecord(pev, pst) == cudaSuccess;
+        if (prev != device) cudaSetDevice(prev);
+        if (!ok) {
+            cudaGetLastError();
+            return BSG_ERR_CUDA;
+        }
+        *launched = true;
+        return BSG_OK;
+    }
+
+    // Admits request q (pool range `off`), writes it into its ring entry and
+    // publishes it (caller holds mu; the entry's previous request,
+    // seq - kRing, is complete).
+    void publish(Request* q, uint64_t off) {
+        q->off = off;
+        q->state = Q_ADMITTED;
+        q->desc.off = off;
+        q->desc.n = q->r.n;
+        q->seq = next_seq++;
+        q->ntiles = (q->r.n + kTile - 1) / kTile;
+        PEntry* e = ring_h + (q->seq & (kRing - 1));
+        e->d = q->desc;
+        e->ntiles = q->ntiles;
+        e->seq = q->seq;
+        __atomic_store_n(&ctl_h->published, next_seq, __ATOMIC_RELEASE);
+        q->t_pub = now_s();
+        pinflight.push_back(q);
+        st.batches++;
+    }
+
+    // Whether request q can be published now (caller holds mu); on success
+    // its pool range is taken.
+    bool can_publish(const Request* q, uint64_t* off) {
+        const uint64_t floor = pinflight.empty() ? next_seq : pinflight.front()->seq;
+        return next_seq < floor + kRing && pool_alloc(q->span, off);
+    }
+
+    void dispatcher_persistent() {
+        std::unique_lock<std::mutex> lk(mu);
+        for (;;) {
+            cv_disp.wait(lk, [&] { return stop || (!paused && !queue.empty()); });
+            if (stop) break;
+            bool published = false;
+            while (!paused && !queue.empty()) {
+                Request* q = queue.front();
+                if (broken) {
+                    queue.pop_front();
+                    complete(q, BSG_ERR_STATE, now_s(), false);
+                    cv_done.notify_all();
+                    continue;
+                }
+                uint64_t off;
+                if (!can_publish(q, &off)) break;  // wait for room
+                queue.pop_front();
+                publish(q, off);
+                published = true;
+            }
+            if (published) {
+                cv_comp.notify_one();  // the completer (re)launches the kernel
+            } else if (!queue.empty() && !paused) {
+                const uint64_t g0 = free_gen;  // wait for a completion to free room
+                cv_disp.wait(lk, [&] { return stop || free_gen != g0 || paused; });
+            }
+        }
+    }
+
+    // Polls the completion flags of published requests (any order), every
+    // few microseconds while any is outstanding, and launches the kernel
+    // whenever requests are outstanding and none is running (first request,
+    // or the kernel exited at its idle bound).  A request older
+    // than batch_timeout fails with BSG_ERR_TIMEOUT and the server turns
+    // broken: its entry may still be written by the GPU, so nothing is reused.
+    void completer_persistent() {
+        set_fine_timer_slack();
+        std::unique_lock<std::mutex> lk(mu);
+        for (;;) {
+            cv_comp.wait(lk, [&] { return stop || !pinflight.empty(); });
+            if (pinflight.empty()) {
+                if (stop) break;
+                continue;
+            }
+            if (!broken) {
+                bool launched = false;
+                lk.unlock();
+                const int krc = ensure_kernel(&launched);
+                lk.lock();
+                if (krc != BSG_OK) broken = true;
+                if (launched) st.kernel_launches++;
+            }
+            const double t = now_s();
+            bool freed = false;
+            for (auto it = pinflight.begin(); it != pinflight.end();) {
+                Request* q = *it;
+                const PEntry* e = ring_h + (q->seq & (kRing - 1));
+                if (__atomic_load_n(&e->flag, __ATOMIC_ACQUIRE) == q->seq + 1) {
+                    complete(q, BSG_OK, t, true);
+                    it = pinflight.erase(it);
+                    freed = true;
+                } else if (t - q->t_pub > batch_timeout) {
+                    broken = true;
+                    complete(q, BSG_ERR_TIMEOUT, t, false);
+                    it = pinflight.erase(it);
+                } else {
+                    ++it;
+                }
+            }
+            if (freed) {
+                free_gen++;
+                cv_done.notify_all();
+                cv_disp.notify_one();
+            }
+            lk.unlock();
+            std::this_thread::sleep_for(std::chrono::microseconds(2));
+            lk.lock();
+        }
+    }
+
     // ------------------------------------------------------- dispatcher
     void dispatcher() {
         cudaSetDevice(device);
+        if (persistent) {
+            dispatcher_persistent();
+            return;
+        }
         std::unique_lock<std::mutex> lk(mu);
         for (;;) {
             cv_disp.wait(lk, [&] { return stop || (!paused && !queue.empty() && free_slot() >= 0); });
@@ -593,6 +922,10 @@ struct bsg_server {
     // -------------------------------------------------------- completer
     void completer() {
         cudaSetDevice(device);
+        if (persistent) {
+            completer_persistent();
+            return;
+        }
         set_fine_timer_slack();
         std::unique_lock<std::mutex> lk(mu);
         for (;;) {
@@ -633,6 +966,24 @@ void destroy_resources(bsg_server* s) {
         if (sl.st) cudaStreamDestroy(sl.st);
     }
     s->slots.clear();
+    if (s->pst) {
+        if (s->ctl_h) __atomic_store_n(&s->ctl_h->stop, 1u, __ATOMIC_RELEASE);
+        cudaStreamSynchronize(s->pst);  // blocks see stop at their next idle check
+        cudaStreamDestroy(s->pst);
+        s->pst = nullptr;
+    }
+    if (s->pev) cudaEventDestroy(s->pev);
+    s->pev = nullptr;
+    if (s->ring_h) cudaFreeHost(s->ring_h);
+    if (s->ctl_h) cudaFreeHost(s->ctl_h);
+    if (s->d_cur) cudaFree(s->d_cur);
+    if (s->d_taken) cudaFree(s->d_taken);
+    if (s->d_done) cudaFree(s->d_done);
+    s->ring_h = nullptr;
+    s->ctl_h = nullptr;
+    s->d_cur = nullptr;
+    s->d_taken = nullptr;
+    s->d_done = nullptr;
     for (auto& h : s->hosts)
         if (h.owned) cudaHostUnregister(reinterpret_cast<void*>(h.b));
     s->hosts.clear();
@@ -648,6 +999,7 @@ int submit_impl(bsg_server* s, const bsg_request* r, uint64_t* id, bool auto_rel
         return BSG_ERR_INVALID_ARG;
     const uint64_t span = (r->n + kAlign - 1) / kAlign * kAlign;
     if (span > s->cap) return BSG_ERR_BUDGET;
+    if (s->persistent && r->n > (uint64_t)kMaxRequestTiles * kTile) return BSG_ERR_CAPACITY;
     Request* q = new (std::nothrow) Request();
     if (!q) return BSG_ERR_OUT_OF_MEMORY;
     q->r = *r;
@@ -675,7 +1027,7 @@ int submit_impl(bsg_server* s, const bsg_request* r, uint64_t* id, bool auto_rel
         }
         q->desc.vec = vec ? 1 : 0;
     }
-    if (s->stop) {
+    if (s->stop || s->broken) {
         delete q;
         return BSG_ERR_STATE;
     }
@@ -689,6 +1041,15 @@ int submit_impl(bsg_server* s, const bsg_request* r, uint64_t* id, bool auto_rel
         return BSG_OK;
     }
     q->state = Q_QUEUED;
+    uint64_t off;
+    if (s->persistent && !s->paused && s->queue.empty() && s->can_publish(q, &off)) {
+        // nothing ahead of it: publish from this thread (no dispatcher hop);
+        // the completer (re)launches the kernel if none is running, so a
+        // submitting thread never waits in the CUDA driver
+        s->publish(q, off);
+        s->cv_comp.notify_one();
+        return BSG_OK;
+    }
     s->queue.push_back(q);
     s->cv_disp.notify_one();
     return BSG_OK;
@@ -727,16 +1088,61 @@ int bsg_server_create(bsg_server** out, const bsg_server_config* cfg) {
         default: delete s; return BSG_ERR_INVALID_ARG;
     }
     s->batch_grid = s->sm_count * bsg::batch_blocks_per_sm();
+    s->persistent = !cfg->plain && cfg->fused == 2;
     int rc = BSG_OK;
     do {
         if (cudaSetDevice(s->device) != cudaSuccess) { rc = BSG_ERR_NO_DEVICE; break; }
         s->cap = cfg->budget_bytes / 28 / kAlign * kAlign;
+        s->free_list[0] = s->cap;
+        if (s->persistent) {
+            // the GPU reads requests from, and counts tiles into, pinned host
+            // memory with system-scope atomics: the host must support them
+            int native = 0;
+            if (cudaDeviceGetAttribute(&native, cudaDevAttrHostNativeAtomicSupported, s->device) !=
+                    cudaSuccess || !native) { rc = BSG_ERR_NOT_SUPPORTED; break; }
+            if (cudaHostAlloc(reinterpret_cast<void**>(&s->ring_h), kRing * sizeof(PEntry),
+                              cudaHostAllocMapped) != cudaSuccess ||
+                cudaHostAlloc(reinterpret_cast<void**>(&s->ctl_h), sizeof(PCtl), cudaHostAllocMapped) !=
+                    cudaSuccess ||
+                cudaMalloc(&s->d_cur, sizeof(unsigned long long)) != cudaSuccess ||
+                cudaMalloc(&s->d_taken, kRing * sizeof(unsigned long long)) != cudaSuccess ||
+                cudaMalloc(&s->d_done, kRing * sizeof(unsigned)) != cudaSuccess) {
+                rc = BSG_ERR_OUT_OF_MEMORY;
+                break;
+            }
+            std::memset(s->ring_h, 0, kRing * sizeof(PEntry));
+            std::memset(s->ctl_h, 0, sizeof(PCtl));
+            // every slot starts armed for the lap before the first: request
+            // i (< kRing) finds tag i - kRing and arms the slot for itself
+            std::vector<unsigned long long> arm(kRing);
+            for (uint64_t i = 0; i < kRing; ++i) arm[i] = (unsigned long long)(uint32_t)(i - kRing) << 32;
+            if (cudaMemcpy(s->d_taken, arm.data(), kRing * sizeof(unsigned long long),
+                           cudaMemcpyHostToDevice) != cudaSuccess ||
+                cudaMemset(s->d_done, 0, kRing * sizeof(unsigned)) != cudaSuccess) {
+                rc = BSG_ERR_CUDA;
+                break;
+            }
+            if (cudaHostGetDevicePointer(reinterpret_cast<void**>(&s->ring_d), s->ring_h, 0) != cudaSuccess ||
+                cudaHostGetDevicePointer(reinterpret_cast<void**>(&s->ctl_d), s->ctl_h, 0) != cudaSuccess ||
+                cudaMemset(s->d_cur, 0, sizeof(unsigned long long)) != cudaSuccess ||
+                cudaStreamCreateWithFlags(&s->pst, cudaStreamNonBlocking) != cudaSuccess ||
+                cudaEventCreateWithFlags(&s->pev, cudaEventDisableTiming) != cudaSuccess ||
+                cudaDeviceSynchronize() != cudaSuccess) {
+                rc = BSG_ERR_CUDA;
+                break;
+            }
+            int occ = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, serve_persistent_kernel<bsg::MODE_FAST>,
+                                                              kThreads, 0) != cudaSuccess || occ < 1)
+                occ = 1;
+            s->pgrid = (unsigned)(s->sm_count * std::min(occ, 3));
+            break;  // no device pool and no batch slots on this path
+        }
         if (cudaMalloc(&s->d_pool, s->cap * 28) != cudaSuccess) { rc = BSG_ERR_OUT_OF_MEMORY; break; }
         float* f = reinterpret_cast<float*>(s->d_pool);
         const uint64_t c = s->cap;
         s->pool = bsg::SoA{f, f + c, f + 2 * c, f + 3 * c, f + 4 * c,
                            reinterpret_cast<const int32_t*>(f + 5 * c), f + 6 * c};
-        s->free_list[0] = c;
         const int nslots = cfg->plain ? 1 : cfg->max_inflight;
         s->slots.resize(nslots);
         const size_t tb = table_bytes(s->max_req);
@@ -781,7 +1187,7 @@ void bsg_server_destroy(bsg_server* s) {
     {
         std::unique_lock<std::mutex> lk(s->mu);
         s->cv_done.wait_for(lk, std::chrono::duration<double>(s->batch_timeout + 1.0),
-                            [&] { return s->inflight.empty(); });
+                            [&] { return s->inflight.empty() && s->pinflight.empty(); });
         s->stop = true;
     }
     s->cv_disp.notify_all();

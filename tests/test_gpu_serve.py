@@ -12,7 +12,9 @@ from p3arsec_gb300.abi import BsgError, Server, serve_trace
 
 pytestmark = pytest.mark.gpu
 
-OK, TIMEOUT, CANCELLED, BUDGET, STATE = 0, -7, -9, -8, -11
+OK, TIMEOUT, CANCELLED, BUDGET, CAPACITY, STATE = 0, -7, -9, -8, -5, -11
+KINDS = {"unfused": dict(fused=False), "fused": dict(fused=True),
+         "persistent": dict(persistent=True)}
 
 
 def pinned_book(torch, n, seed):
@@ -35,8 +37,8 @@ def disjoint_requests(rng, pool_n, count, max_n):
     return reqs
 
 
-@pytest.mark.parametrize("fused", [False, True])
-def test_each_result_same_alone_and_in_mix(gpu_ctx, fused):
+@pytest.mark.parametrize("kind", list(KINDS))
+def test_each_result_same_alone_and_in_mix(gpu_ctx, kind):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(5)
     pool_n = 1 << 21
@@ -44,7 +46,7 @@ def test_each_result_same_alone_and_in_mix(gpu_ctx, fused):
     mix = pinned_zeros(torch, pool_n)
     alone = pinned_zeros(torch, pool_n)
     reqs = disjoint_requests(rng, pool_n, 400, 40000)
-    with Server(budget_bytes=256 << 20, max_inflight=4, fused=fused) as srv:
+    with Server(budget_bytes=256 << 20, max_inflight=4, **KINDS[kind]) as srv:
         for a in host + [mix, alone]:
             srv.register(a)
         # the mix: four threads submit concurrently while admission is held,
@@ -68,10 +70,15 @@ def test_each_result_same_alone_and_in_mix(gpu_ctx, fused):
             assert st == OK and lat > 0
         stats = srv.stats()
         assert stats["completed"] == len(reqs)
-        assert stats["batches"] < len(reqs) / 4  # requests were coalesced
-        # batches of more than 24 requests take the copied-table launch, the
-        # single requests below the table-in-parameters launch
-        assert stats["max_batch_requests_seen"] > 24
+        if kind == "persistent":
+            # every request went to the one running kernel (relaunched at
+            # most after an idle exit), none needed a launch of its own
+            assert stats["kernel_launches"] <= 3
+        else:
+            assert stats["batches"] < len(reqs) / 4  # requests were coalesced
+            # batches of more than 24 requests take the copied-table launch,
+            # the single requests below the table-in-parameters launch
+            assert stats["max_batch_requests_seen"] > 24
         # alone: one request in flight at a time
         for o, n in reqs[:50]:
             st, _ = srv.wait(srv.submit(*[a[o:] for a in host], alone[o:], n=n), timeout_s=60.0)
@@ -120,13 +127,14 @@ def test_cancel_and_bounded_wait():
         assert srv.cancel(srv.submit(*host, out, n=10)) in (OK, STATE)
 
 
-def test_admission_by_budget():
+@pytest.mark.parametrize("kind", ["fused", "persistent"])
+def test_admission_by_budget(gpu_ctx, kind):
     torch = pytest.importorskip("torch")
     pool_n = 600000
     book, host = pinned_book(torch, pool_n, 44)
     out = pinned_zeros(torch, pool_n)
     budget = 28 * 131072  # room for one 100k request at a time
-    with Server(budget_bytes=budget, max_inflight=4) as srv:
+    with Server(budget_bytes=budget, max_inflight=4, **KINDS[kind]) as srv:
         for a in host + [out]:
             srv.register(a)
         with pytest.raises(BsgError) as e:
@@ -136,7 +144,10 @@ def test_admission_by_budget():
                for o in range(0, 500000, 100000)]
         for rid in ids:
             assert srv.wait(rid, timeout_s=60.0)[0] == OK
-        assert srv.stats()["max_batch_requests_seen"] == 1
+        if kind == "fused":
+            assert srv.stats()["max_batch_requests_seen"] == 1
+    ref = gpu_ctx.price_book(book)
+    assert np.array_equal(out[:500000].view(np.uint32), ref[:500000].view(np.uint32))
 
 
 def test_unregistered_host_memory_is_rejected():
@@ -151,16 +162,53 @@ def test_unregistered_host_memory_is_rejected():
         assert srv.lib.bsg_server_register(srv.h, pinned.data_ptr(), 1 << 30) != 0
 
 
-@pytest.mark.parametrize("plain,fused", [(False, False), (False, True), (True, False)])
-def test_short_trace(plain, fused):
+@pytest.mark.parametrize("plain,kind", [(False, "unfused"), (False, "fused"),
+                                        (False, "persistent"), (True, "unfused")])
+def test_short_trace(plain, kind):
     torch = pytest.importorskip("torch")
     pool_n = 1 << 20
     _, host = pinned_book(torch, pool_n, 46)
     out = pinned_zeros(torch, pool_n)
     lat = np.zeros(5000)
     res = serve_trace(host, out, rate_per_s=1000, duration_s=0.5, min_n=16, max_n=1 << 16,
-                      seed=3, budget_bytes=1 << 30, plain=plain, latencies=lat, fused=fused)
+                      seed=3, budget_bytes=1 << 30, plain=plain, latencies=lat, **KINDS[kind])
     assert res["requests"] > 300
     assert res["completed"] == res["requests"]
     assert 0 < res["p50_s"] <= res["p99_s"] <= res["max_s"] < 10
     assert np.isfinite(lat[:res["requests"]]).all()
+
+
+def test_persistent_kernel_exits_when_idle_and_relaunches(gpu_ctx):
+    """The persistent kernel's only wait (for published work) is bounded:
+    with nothing published for longer than its 5 ms bound every block exits
+    by itself (a host-side omission, no fault); the next request relaunches
+    the kernel and completes."""
+    import time
+    torch = pytest.importorskip("torch")
+    book, host = pinned_book(torch, 300000, 47)
+    out = pinned_zeros(torch, 300000)
+    with Server(budget_bytes=64 << 20, persistent=True) as srv:
+        for a in host + [out]:
+            srv.register(a)
+        assert srv.wait(srv.submit(*host, out, n=100000), timeout_s=60.0)[0] == OK
+        assert srv.stats()["kernel_launches"] == 1
+        time.sleep(0.05)  # ten idle bounds: the kernel has exited
+        assert srv.wait(srv.submit(*[a[100000:] for a in host], out[100000:], n=200000),
+                        timeout_s=60.0)[0] == OK
+        assert srv.stats()["kernel_launches"] == 2
+    ref = gpu_ctx.price_book(book)
+    assert np.array_equal(out.view(np.uint32), ref.view(np.uint32))
+
+
+def test_persistent_request_size_limit():
+    torch = pytest.importorskip("torch")
+    _, host = pinned_book(torch, 1000, 48)
+    out = pinned_zeros(torch, 1000)
+    with Server(budget_bytes=1 << 30, persistent=True) as srv:
+        for a in host + [out]:
+            srv.register(a)
+        # checked before any array is touched: 4095 tiles of 2048 options
+        with pytest.raises(BsgError) as e:
+            srv.submit(*host, out, n=4095 * 2048 + 1)
+        assert e.value.status == CAPACITY
+        assert srv.wait(srv.submit(*host, out, n=1000), timeout_s=60.0)[0] == OK
