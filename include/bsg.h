@@ -273,7 +273,9 @@ typedef struct bsg_request {
 
 typedef struct bsg_server_stats {
     uint64_t submitted, completed, cancelled, failed;
-    uint64_t batches, kernel_launches, options_priced;
+    uint64_t batches;          /* batches launched (persistent path: requests published) */
+    uint64_t kernel_launches;  /* persistent path: launches of the persistent kernel */
+    uint64_t options_priced;
     uint64_t max_batch_requests_seen;
     uint64_t queued, inflight_requests;
 } bsg_server_stats;

@@ -1296,7 +1296,7 @@ int bsg_server_get_stats(bsg_server* s, bsg_server_stats* out) {
     std::lock_guard<std::mutex> lk(s->mu);
     *out = s->st;
     out->queued = s->queue.size();
-    uint64_t in = 0;
+    uint64_t in = s->pinflight.size();  // persistent path: published, not complete
     for (int si : s->inflight) in += s->slots[si].reqs.size();
     out->inflight_requests = in;
     return BSG_OK;
