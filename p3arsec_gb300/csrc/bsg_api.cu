@@ -1090,7 +1090,11 @@ static std::string tune_key(const bsg_ctx* c, size_t n) {
     return os.str();
 }
 
+// Serialises this process's reads and appends of the tuning cache file.
+static std::mutex g_tune_cache_mu;
+
 static bool tune_cache_lookup(const std::string& key, bsg_tune* t) {
+    std::lock_guard<std::mutex> lk(g_tune_cache_mu);
     const char* path = std::getenv("BSG_TUNE_CACHE");
     if (!path || !*path) return false;
     std::ifstream f(path);
@@ -1110,6 +1114,7 @@ static bool tune_cache_lookup(const std::string& key, bsg_tune* t) {
 }
 
 static void tune_cache_store(const std::string& key, const bsg_tune& t) {
+    std::lock_guard<std::mutex> lk(g_tune_cache_mu);
     const char* path = std::getenv("BSG_TUNE_CACHE");
     if (!path || !*path) return;
     std::ofstream f(path, std::ios::app);

@@ -17,6 +17,8 @@
 #include "bsg_internal.h"
 #include "bsg_math.cuh"
 
+#include <atomic>
+
 namespace bsg {
 
 // ------------------------------------------------------------ memory access
@@ -376,16 +378,18 @@ static cudaError_t launch_map_bulk(const SoA& a, int64_t n, const MapCfg& cfg, i
                                   cudaStream_t st, uint64_t wait_ns = kBulkWaitNs,
                                   uint32_t tx_extra = 0) {
     using B = BulkShape<OPT, STAGES>;
-    // opt in to the dynamic shared memory, once per device
-    static unsigned long long opted = 0;
+    // opt in to the dynamic shared memory, once per device (contexts on
+    // several host threads may race here: setting the attribute twice is
+    // harmless, the bit mask is atomic)
+    static std::atomic<unsigned long long> opted{0};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    if (dev < 64 && !(opted & (1ull << dev))) {
+    if (dev >= 64 || !(opted.load(std::memory_order_acquire) & (1ull << dev))) {
         e = cudaFuncSetAttribute(map_bulk_kernel<M, OPT, STAGES>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, B::smem);
         if (e != cudaSuccess) return e;
-        opted |= 1ull << dev;
+        if (dev < 64) opted.fetch_or(1ull << dev, std::memory_order_release);
     }
     const int64_t ntiles = n / B::tile;
     int64_t grid = (int64_t)sm_count * (220 * 1024 / B::smem);  // CTAs that fit per SM
