@@ -1138,11 +1138,15 @@ int bsg_server_create(bsg_server** out, const bsg_server_config* cfg) {
             s->pgrid = (unsigned)(s->sm_count * std::min(occ, 3));
             break;  // no device pool and no batch slots on this path
         }
-        if (cudaMalloc(&s->d_pool, s->cap * 28) != cudaSuccess) { rc = BSG_ERR_OUT_OF_MEMORY; break; }
-        float* f = reinterpret_cast<float*>(s->d_pool);
-        const uint64_t c = s->cap;
-        s->pool = bsg::SoA{f, f + c, f + 2 * c, f + 3 * c, f + 4 * c,
-                           reinterpret_cast<const int32_t*>(f + 5 * c), f + 6 * c};
+        // the device pool holds requests only on the unfused and plain paths;
+        // the fused kernel reads and writes host memory in place
+        if (cfg->plain || cfg->fused == 0) {
+            if (cudaMalloc(&s->d_pool, s->cap * 28) != cudaSuccess) { rc = BSG_ERR_OUT_OF_MEMORY; break; }
+            float* f = reinterpret_cast<float*>(s->d_pool);
+            const uint64_t c = s->cap;
+            s->pool = bsg::SoA{f, f + c, f + 2 * c, f + 3 * c, f + 4 * c,
+                               reinterpret_cast<const int32_t*>(f + 5 * c), f + 6 * c};
+        }
         const int nslots = cfg->plain ? 1 : cfg->max_inflight;
         s->slots.resize(nslots);
         const size_t tb = table_bytes(s->max_req);
