@@ -20,6 +20,7 @@
 #include "bsg.h"
 #include "bsg_internal.h"
 #include "bsg_math.cuh"
+#include "bsg_ring.h"
 
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -296,7 +297,7 @@ cudaError_t launch_fused_inline(int mode, unsigned grid, cudaStream_t st, const 
 // published work: bounded by idle_ns of GPU time (and the host's stop
 // flag), after which the block exits; the host relaunches the kernel when
 // work arrives and no kernel is running.
-constexpr uint32_t kMaxRequestTiles = 4095;  // 12 bits of the claim word
+constexpr uint64_t kMaxRequestTiles = bsg_ring::kMaxTiles;  // 12 bits of the claim word
 
 struct alignas(128) PEntry {
     unsigned long long flag;    // seq + 1 once every tile is priced (GPU writes)
@@ -340,6 +341,23 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
+// The claim protocol's memory operations on the device (bsg_ring.h): claim
+// words and done counts in device memory, tile counts from the published
+// entries in host memory.
+struct DeviceRingOps {
+    unsigned long long* taken;
+    unsigned* done;
+    const PEntry* ring;
+    __device__ uint64_t load(uint64_t s) { return ld_relaxed_gpu(taken + s); }
+    __device__ uint64_t cas(uint64_t s, uint64_t expect, uint64_t want) {
+        return atomicCAS(taken + s, (unsigned long long)expect, (unsigned long long)want);
+    }
+    __device__ uint64_t add(uint64_t s) { return atomicAdd(taken + s, 1ull); }
+    __device__ uint64_t ntiles(uint64_t s) { return ring[s].ntiles; }
+    __device__ uint64_t done_add(uint64_t s) { return atom_add_acq_rel_gpu(done + s, 1u); }
+    __device__ void done_reset(uint64_t s) { done[s] = 0u; }
+};
+
 template <int M>
 __global__ void __launch_bounds__(kThreads) serve_persistent_kernel(
     PEntry* ring, unsigned long long rmask, const PCtl* ctl, unsigned long long* cur,
@@ -364,45 +382,27 @@ __global__ void __launch_bounds__(kThreads) serve_persistent_kernel(
                     if (backoff < 8192) backoff *= 2;
                     continue;
                 }
-                const unsigned long long slot = r & rmask;
-                const unsigned tag = (unsigned)r;
-                unsigned long long w = ld_relaxed_gpu(taken + slot);
-                bool advance = false;
-                for (;;) {
-                    const int lap = (int)((unsigned)(w >> 32) - tag);
-                    if (lap < 0) {  // slot still armed for the previous lap: arm it for r
-                        const unsigned long long nt = ring[slot].ntiles;  // published entry r
-                        const unsigned long long want = (unsigned long long)tag << 32 | nt << 20;
-                        const unsigned long long seen = atomicCAS(taken + slot, w, want);
-                        w = (seen == w) ? want : seen;
-                        continue;
+                DeviceRingOps ops{taken, done, ring};
+                uint64_t q = 0, c = 0, nt = 0;
+                if (bsg_ring::claim(ops, r, rmask, &q, &c, &nt) == bsg_ring::kTile) {
+                    // a tile of q: r, or a later request of the same slot,
+                    // which another block armed after seeing it published;
+                    // see that publication here too before reading q's entry
+                    // (bounded: it happened before the arming)
+                    for (int i = 0; q >= pub && i < (1 << 20); ++i)
+                        pub = ld_acquire_sys(&ctl->published);
+                    const unsigned long long slot = q & rmask;
+                    if (d_seq != q) {  // consecutive tiles of one request: read once
+                        sh_d = ring[slot].d;
+                        d_seq = q;
                     }
-                    if (lap > 0) {  // a later lap: request r is finished
-                        advance = true;
-                        break;
-                    }
-                    const unsigned long long old = atomicAdd(taken + slot, 1ull);
-                    if ((unsigned)(old >> 32) != tag) {  // re-armed meanwhile
-                        w = old;
-                        continue;
-                    }
-                    const unsigned long long c = old & 0xFFFFFull, nt = (old >> 20) & 0xFFFull;
-                    if (c < nt) {  // tile c of request r
-                        if (d_seq != r) {  // consecutive tiles of one request: read once
-                            sh_d = ring[slot].d;
-                            d_seq = r;
-                        }
-                        sh_b = c * kTile;
-                        sh_seq = r;
-                        sh_nt = nt;
-                        sh_ok = 1;
-                    } else {
-                        advance = true;  // every tile of r is claimed
-                    }
+                    sh_b = c * kTile;
+                    sh_seq = q;
+                    sh_nt = nt;
+                    sh_ok = 1;
                     break;
                 }
-                if (sh_ok) break;
-                if (advance) atomicCAS(cur, r, r + 1);
+                atomicCAS(cur, r, r + 1);  // r has no unclaimed tile: move on
                 t0 = global_ns();
                 backoff = 64;
             }
@@ -414,13 +414,11 @@ __global__ void __launch_bounds__(kThreads) serve_persistent_kernel(
         __threadfence_system();  // this thread's prices reach host memory first
         __syncthreads();
         if (threadIdx.x == 0) {
+            // the request's last tile: every block's prices are in host
+            // memory (each fenced before its count); the count is re-armed
+            DeviceRingOps ops{taken, done, ring};
             const unsigned long long slot = sh_seq & rmask;
-            if (atom_add_acq_rel_gpu(done + slot, 1u) + 1u == (unsigned)sh_nt) {
-                // the request's last tile: every block's prices are in host
-                // memory (each fenced before its count); re-arm the count
-                done[slot] = 0u;
-                st_release_sys(&ring[slot].flag, sh_seq + 1ull);
-            }
+            if (bsg_ring::finish(ops, slot, sh_nt)) st_release_sys(&ring[slot].flag, sh_seq + 1ull);
         }
     }
 }
@@ -1115,7 +1113,7 @@ int bsg_server_create(bsg_server** out, const bsg_server_config* cfg) {
             // every slot starts armed for the lap before the first: request
             // i (< kRing) finds tag i - kRing and arms the slot for itself
             std::vector<unsigned long long> arm(kRing);
-            for (uint64_t i = 0; i < kRing; ++i) arm[i] = (unsigned long long)(uint32_t)(i - kRing) << 32;
+            for (uint64_t i = 0; i < kRing; ++i) arm[i] = bsg_ring::initial_word(i, kRing);
             if (cudaMemcpy(s->d_taken, arm.data(), kRing * sizeof(unsigned long long),
                            cudaMemcpyHostToDevice) != cudaSuccess ||
                 cudaMemset(s->d_done, 0, kRing * sizeof(unsigned)) != cudaSuccess) {
