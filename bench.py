@@ -89,13 +89,15 @@ def reduce_max(dist, x: float, device=None) -> float:
 
 
 # ----------------------------------------------------------------- clocks
-CLOCK_QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+CLOCK_QUERY = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
 
 class ClockSampler:
-    """nvidia-smi samples every 200 ms while the timed region runs."""
+    """nvidia-smi samples every 50 ms around the timed region; the summary
+    keeps the samples whose timestamps fall inside it (all samples, with
+    window_samples = 0, if the region was shorter than the sampling gap)."""
 
     def __init__(self, device: int):
         self.device = device
@@ -108,16 +110,18 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={CLOCK_QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
             time.sleep(0.3)
         except OSError:
             self.proc = None
+        self.t0 = time.time()
         return self
 
     def __exit__(self, *exc):
+        self.t1 = time.time()
         if self.proc is not None:
-            time.sleep(0.25)
+            time.sleep(0.12)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -127,21 +131,29 @@ class ClockSampler:
     def summary(self):
         if not self.path or not os.path.exists(self.path):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        import datetime
         rows = []
         for line in open(self.path):
             f = [x.strip() for x in line.split(",")]
-            if len(f) >= 9:
-                rows.append(f)
+            if len(f) >= 10:
+                try:
+                    f[0] = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                except ValueError:
+                    continue
+                rows.append(f[:1] + f[2:])  # drop the index column
         os.unlink(self.path)
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        inside = [r for r in rows if self.t0 - 0.01 <= r[0] <= self.t1 + 0.01]
+        use = inside if inside else rows
+        sm = [float(r[1]) for r in use if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in use if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        reasons = sorted({names[i] for r in use for i in range(4) if r[5 + i].lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(rows)}
+                "samples": len(use), "window_samples": len(inside),
+                "window_s": round(self.t1 - self.t0, 4)}
 
 
 def measured_hbm_peak():
@@ -675,7 +687,9 @@ def run_reference(args, rank, world, local):
     book = books.generate(n, seed=SEED)
     threads = os.cpu_count() or 1
     _, t1 = oracle.bs_map(book, threads, 1)
-    runs = int(max(1, min(args.runs, round(2.0 / max(t1, 1e-6)))))
+    # each step a bounded sample: ~2 s of CPU work, less when many steps are
+    # asked for, so that the whole run stays near a minute
+    runs = int(max(1, min(args.runs, round(min(2.0, 60.0 / args.steps) / max(t1, 1e-6)))))
     for _ in range(args.warmup):
         oracle.bs_map(book, threads, runs)
     total = 0.0
@@ -702,7 +716,8 @@ def run_reference(args, rank, world, local):
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 100 for the map, 10 otherwise)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", choices=["map", "batch", "precision", "serve", "io", "fp64"],
@@ -729,6 +744,8 @@ def main(argv=None):
     ap.add_argument("--tune", default=None,
                     help="vec_per_thread,block,blocks_per_sm,load_path[,pdl] instead of autotuning")
     args = ap.parse_args(argv)
+    if args.steps is None:
+        args.steps = 100 if (args.config == "map" and args.impl == "ours") else 10
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
     rank, world, local = dist_env()
