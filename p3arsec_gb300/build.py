@@ -58,8 +58,23 @@ def _headers():
 
 
 def build(verbose: bool = False, force: bool = False) -> str:
-    """Build libbsgpu.so and the CLI if stale; returns the library path."""
+    """Build libbsgpu.so and the CLI if stale; returns the library path.
+
+    Processes building at once (one per rank under torchrun) take turns on a
+    lock file, and the library and CLI are linked to a temporary name and
+    renamed into place, so a process that has the library loaded never sees
+    it rewritten."""
     os.makedirs(BUILD, exist_ok=True)
+    import fcntl
+    with open(os.path.join(BUILD, ".build.lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        try:
+            return _build_locked(verbose, force)
+        finally:
+            fcntl.flock(lock, fcntl.LOCK_UN)
+
+
+def _build_locked(verbose: bool, force: bool) -> str:
     nv = nvcc()
     heads = _headers()
     jobs = []
@@ -85,13 +100,17 @@ def build(verbose: bool = False, force: bool = False) -> str:
                 if verbose and out.strip():
                     print(out)
     if force or jobs or _stale(LIB, objs):
-        _run([nv] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread"])
+        tmp = LIB + ".tmp"
+        _run([nv] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"])
+        os.replace(tmp, LIB)
     cli_src = os.path.join(HOST, "blackscholes_gpu.cpp")
     if os.path.exists(cli_src) and (force or _stale(CLI, [cli_src, LIB] + heads)):
         os.makedirs(os.path.dirname(CLI), exist_ok=True)
+        tmp = CLI + ".tmp"
         _run(["g++", "-O2", "-std=c++17", "-Wall", "-I" + os.path.join(ROOT, "include"),
-              cli_src, "-o", CLI, "-L" + PKG, "-lbsgpu", "-Wl,-rpath,$ORIGIN/..",
+              cli_src, "-o", tmp, "-L" + PKG, "-lbsgpu", "-Wl,-rpath,$ORIGIN/..",
               "-lpthread"])
+        os.replace(tmp, CLI)
     return LIB
 
 
