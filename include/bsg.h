@@ -332,7 +332,8 @@ typedef struct bsg_trace_result {
     double p50_s, p99_s, p999_s, max_s, mean_s;
     double mean_batch_requests;
     uint64_t batches;
-    double late_submit_max_s; /* how far behind schedule the submitter fell */
+    double late_submit_max_s; /* how far behind schedule the submitter fell
+                                 (BSG_TRACE_DEBUG=1 prints which request) */
 } bsg_trace_result;
 
 int bsg_serve_trace(const bsg_server_config* cfg, const bsg_trace_config* trace,

@@ -29,6 +29,8 @@
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -322,6 +324,11 @@ __device__ __forceinline__ unsigned ld_relaxed_sys_u32(const unsigned* p) {
     asm volatile("ld.relaxed.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+__device__ __forceinline__ unsigned long long ld_acquire_gpu(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
 __device__ __forceinline__ unsigned long long ld_relaxed_gpu(const unsigned long long* p) {
     unsigned long long v;
     asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
@@ -366,20 +373,36 @@ __global__ void __launch_bounds__(kThreads) serve_persistent_kernel(
     __shared__ unsigned long long sh_b, sh_seq, sh_nt;
     __shared__ int sh_ok;
     // thread 0's view of `published` (re-read from host memory only when the
-    // ring looks drained) and the request whose descriptor sh_d holds
+    // ring looks drained) and the request whose descriptor sh_d holds.  While
+    // idle, only the first kScouts blocks poll host memory; they copy what
+    // they see into a device word (cur[1]) that the other blocks poll in L2,
+    // so every block notices new work within about a microsecond without
+    // hundreds of blocks reading across the link.
+    constexpr unsigned kScouts = 8;
+    const bool scout = blockIdx.x < kScouts;
+    unsigned long long* pub_dev = cur + 1;
     unsigned long long pub = 0, d_seq = ~0ull;
     for (;;) {
         if (threadIdx.x == 0) {
             sh_ok = 0;
-            unsigned backoff = 64;
+            unsigned backoff = 64, polls = 0;
             unsigned long long t0 = global_ns();
             while (ld_relaxed_sys_u32(&ctl->stop) == 0) {
                 const unsigned long long r = ld_relaxed_gpu(cur);
-                if (r >= pub) pub = ld_acquire_sys(&ctl->published);
+                if (r >= pub) {
+                    // (a non-scout also reads the host's count itself every
+                    // 32nd poll, in case every scout is busy pricing)
+                    if (scout || (++polls & 31) == 0) {
+                        pub = ld_acquire_sys(&ctl->published);
+                        if (pub > r) atomicMax(pub_dev, pub);
+                    } else if (ld_acquire_gpu(pub_dev) > r) {
+                        pub = ld_acquire_sys(&ctl->published);  // see the entries too
+                    }
+                }
                 if (r >= pub) {  // nothing published
                     if (global_ns() - t0 > idle_ns) break;  // bounded idle wait
                     __nanosleep(backoff);
-                    if (backoff < 8192) backoff *= 2;
+                    if (backoff < 1024) backoff *= 2;
                     continue;
                 }
                 DeviceRingOps ops{taken, done, ring};
@@ -511,6 +534,7 @@ size_t table_bytes(int cap) {
 
 constexpr uint64_t kRing = 4096;                 // persistent ring entries
 constexpr unsigned long long kIdleNs = 5000000;  // a block's idle bound: 5 ms
+constexpr double kPollWindow = 5e-3;             // completer polls this long after work
 
 struct bsg_server {
     bsg_server_config cfg{};
@@ -523,7 +547,9 @@ struct bsg_server {
     PEntry* ring_d = nullptr;
     PCtl* ctl_h = nullptr;
     PCtl* ctl_d = nullptr;
-    unsigned long long* d_cur = nullptr;  // oldest request that may have unclaimed tiles
+    // device words: [0] the oldest request that may have unclaimed tiles,
+    // [1] the scouts' copy of `published` (see serve_persistent_kernel)
+    unsigned long long* d_cur = nullptr;
     unsigned long long* d_taken = nullptr;  // per ring slot: claim word
     unsigned* d_done = nullptr;             // per ring slot: tiles priced
     cudaStream_t pst = nullptr;
@@ -794,8 +820,18 @@ struct bsg_server {
     void completer_persistent() {
         set_fine_timer_slack();
         std::unique_lock<std::mutex> lk(mu);
+        double last_busy = now_s();
         for (;;) {
+            // for a while after the last request, keep polling instead of
+            // sleeping on the condition variable: a thread woken from it
+            // starts tens of microseconds late, the poll within a few
+            while (!stop && pinflight.empty() && now_s() - last_busy < kPollWindow) {
+                lk.unlock();
+                std::this_thread::sleep_for(std::chrono::microseconds(2));
+                lk.lock();
+            }
             cv_comp.wait(lk, [&] { return stop || !pinflight.empty(); });
+            last_busy = now_s();
             if (pinflight.empty()) {
                 if (stop) break;
                 continue;
@@ -1102,7 +1138,7 @@ int bsg_server_create(bsg_server** out, const bsg_server_config* cfg) {
                               cudaHostAllocMapped) != cudaSuccess ||
                 cudaHostAlloc(reinterpret_cast<void**>(&s->ctl_h), sizeof(PCtl), cudaHostAllocMapped) !=
                     cudaSuccess ||
-                cudaMalloc(&s->d_cur, sizeof(unsigned long long)) != cudaSuccess ||
+                cudaMalloc(&s->d_cur, 2 * sizeof(unsigned long long)) != cudaSuccess ||
                 cudaMalloc(&s->d_taken, kRing * sizeof(unsigned long long)) != cudaSuccess ||
                 cudaMalloc(&s->d_done, kRing * sizeof(unsigned)) != cudaSuccess) {
                 rc = BSG_ERR_OUT_OF_MEMORY;
@@ -1122,7 +1158,7 @@ int bsg_server_create(bsg_server** out, const bsg_server_config* cfg) {
             }
             if (cudaHostGetDevicePointer(reinterpret_cast<void**>(&s->ring_d), s->ring_h, 0) != cudaSuccess ||
                 cudaHostGetDevicePointer(reinterpret_cast<void**>(&s->ctl_d), s->ctl_h, 0) != cudaSuccess ||
-                cudaMemset(s->d_cur, 0, sizeof(unsigned long long)) != cudaSuccess ||
+                cudaMemset(s->d_cur, 0, 2 * sizeof(unsigned long long)) != cudaSuccess ||
                 cudaStreamCreateWithFlags(&s->pst, cudaStreamNonBlocking) != cudaSuccess ||
                 cudaEventCreateWithFlags(&s->pev, cudaEventDisableTiming) != cudaSuccess ||
                 cudaDeviceSynchronize() != cudaSuccess) {
@@ -1343,6 +1379,7 @@ int bsg_serve_trace(const bsg_server_config* cfg, const bsg_trace_config* tr,
     }
     const double t0 = now_s() + 0.02;
     double late = 0.0;
+    size_t late_at = 0;
     uint64_t submitted = 0;
     for (size_t k = 0; k < count; ++k) {
         const double ts = t0 + at[k];
@@ -1352,8 +1389,9 @@ int bsg_serve_trace(const bsg_server_config* cfg, const bsg_trace_config* tr,
                 std::this_thread::sleep_for(std::chrono::duration<double>(ts - tn - 100e-6));
             while (now_s() < ts) {
             }
-        } else {
-            late = std::max(late, tn - ts);
+        } else if (tn - ts > late) {
+            late = tn - ts;
+            late_at = k;
         }
         const uint64_t o = offs[k];
         bsg_request r{tr->sptprice + o, tr->strike + o, tr->rate + o, tr->volatility + o,
@@ -1368,6 +1406,10 @@ int bsg_serve_trace(const bsg_server_config* cfg, const bsg_trace_config* tr,
             return s->st.completed + s->st.failed + s->st.cancelled >= submitted;
         });
     }
+    if (const char* dbg = std::getenv("BSG_TRACE_DEBUG"); dbg && *dbg == '1')
+        std::fprintf(stderr, "bsg_serve_trace: submitter at most %.3f ms late, at request %zu of %zu "
+                             "(scheduled %.3f s into the trace)\n",
+                     late * 1e3, late_at, count, count ? at[late_at] : 0.0);
     bsg_server_stats stt;
     bsg_server_get_stats(s, &stt);
     bsg_server_destroy(s);  // cancels anything left
