@@ -736,7 +736,7 @@ def main(argv=None):
     ap.add_argument("--books", type=int, default=4096, help="batch config: number of books")
     ap.add_argument("--batch-tune", default=None,
                     help="batch config: tile_options,blocks_per_sm instead of autotuning")
-    ap.add_argument("--n", type=int, default=N_OPTIONS)
+    ap.add_argument("--n", "--options", dest="n", type=int, default=N_OPTIONS)
     ap.add_argument("--runs", type=int, default=NUM_RUNS)
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
