@@ -4,9 +4,11 @@
 // "%f %f %f %f %f %f %c %f %f" = s strike r divq v t OptionType divs DGrefval.
 // Output (blackscholes.c:923-947): "%i\n" then "%.18f\n" per price.
 //
-// The parser converts every float with strtof (what glibc's scanf "%f" does:
-// round to nearest), so arrays are bit-identical to the reference's.  It
-// splits the text at line starts and parses the chunks on nthreads threads;
+// The parser converts every float to the value glibc's scanf "%f" (strtof,
+// round to nearest) gives, so arrays are bit-identical to the reference's:
+// plain decimals of up to 19 significant digits take an exact fast path
+// (below), everything else goes to strtof.  It splits the text at line
+// starts and parses the chunks on nthreads threads;
 // when a chunk does not hold whole 9-field records (a record spread over
 // lines) it falls back to one sequential pass.  The writer formats "%.18f"
 // exactly with integer arithmetic (round half to even, as glibc's printf
@@ -14,11 +16,18 @@
 // snprintf for non-finite values and |x| >= 2^40.
 #include "bsg.h"
 
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <cerrno>
+#include <cfloat>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
+#include <new>
 #include <string>
 #include <thread>
 #include <vector>
@@ -38,10 +47,95 @@ inline void skip_ws(Cursor& c) {
     while (c.p < c.end && is_space(*c.p)) ++c.p;
 }
 
-// One "%f": strtof on the next token (the buffer is NUL-terminated).
+// Exact decimal -> float fast path (Clinger's method).  For a token
+// [+-]digits[.digits][(e|E)[+-]digits] with at most 19 significant digits,
+// the value is m x 10^e10 with m an integer:
+//  * m <= 2^24 and |e10| <= 10: m and 10^|e10| are exact floats, so one
+//    correctly rounded float multiply or divide gives the correctly rounded
+//    result;
+//  * m <= 2^53 and |e10| <= 22: the same in double gives the correctly
+//    rounded double d; rounding d to float is then correct unless d lies
+//    exactly halfway between two floats (the decimal value may not), or d
+//    is outside the normal float range: those go to strtof.
+// Returns false (nothing consumed) when the token needs strtof.
+const float kPow10f[11] = {1e0f, 1e1f, 1e2f, 1e3f, 1e4f, 1e5f, 1e6f, 1e7f, 1e8f, 1e9f, 1e10f};
+const double kPow10d[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8,  1e9,  1e10, 1e11,
+                            1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+
+inline bool is_digit(char ch) { return ch >= '0' && ch <= '9'; }
+
+inline bool fast_float(const char* p, const char* end, float* out, const char** stop) {
+    const char* q = p;
+    bool neg = false;
+    if (q < end && (*q == '+' || *q == '-')) neg = (*q++ == '-');
+    uint64_t m = 0;
+    int sig = 0, e10 = 0;
+    bool any = false;
+    while (q < end && is_digit(*q)) {
+        any = true;
+        if (m == 0 && *q == '0') { ++q; continue; }  // leading zeros
+        if (++sig > 19) return false;
+        m = m * 10 + (uint64_t)(*q++ - '0');
+    }
+    if (q < end && *q == '.') {
+        ++q;
+        while (q < end && is_digit(*q)) {
+            any = true;
+            --e10;
+            if (m == 0 && *q == '0') { ++q; continue; }
+            if (++sig > 19) return false;
+            m = m * 10 + (uint64_t)(*q++ - '0');
+        }
+    }
+    if (!any) return false;  // no digits (inf, nan, ".", hex, ...): strtof decides
+    if (q < end && (*q == 'x' || *q == 'X')) return false;  // "0x..." hexadecimal
+    if (q < end && (*q == 'e' || *q == 'E')) {
+        const char* r = q + 1;
+        bool eneg = false;
+        if (r < end && (*r == '+' || *r == '-')) eneg = (*r++ == '-');
+        if (r < end && is_digit(*r)) {  // else the 'e' is not part of the number
+            int ex = 0;
+            while (r < end && is_digit(*r)) {
+                if (ex > 10000) return false;
+                ex = ex * 10 + (*r++ - '0');
+            }
+            e10 += eneg ? -ex : ex;
+            q = r;
+        }
+    }
+    float v;
+    if (m == 0) {
+        v = 0.0f;
+    } else if (m <= (1ull << 24) && e10 >= -10 && e10 <= 10) {
+        v = (float)m;
+        v = e10 >= 0 ? v * kPow10f[e10] : v / kPow10f[-e10];
+    } else if (m <= (1ull << 53) && e10 >= -22 && e10 <= 22) {
+        double d = (double)m;
+        d = e10 >= 0 ? d * kPow10d[e10] : d / kPow10d[-e10];
+        if (!(d >= (double)FLT_MIN && d <= (double)FLT_MAX)) return false;
+        v = (float)d;
+        if ((double)v != d) {  // inexact: a tie in double may not be one in decimal
+            const float w = std::nextafter(v, (double)v < d ? FLT_MAX : 0.0f);
+            if (d == ((double)v + (double)w) * 0.5) return false;
+        }
+    } else {
+        return false;
+    }
+    *out = neg ? -v : v;
+    *stop = q;
+    return true;
+}
+
+// One "%f": the fast path, else strtof on the next token (the buffer is
+// NUL-terminated).
 inline bool read_float(Cursor& c, float* out) {
     skip_ws(c);
     if (c.p >= c.end) return false;
+    const char* stop = nullptr;
+    if (fast_float(c.p, c.end, out, &stop)) {
+        c.p = stop;
+        return true;
+    }
     char* e = nullptr;
     const float v = std::strtof(c.p, &e);
     if (e == c.p) return false;
@@ -255,33 +349,61 @@ int bsg_parse_parsec(const char* text, size_t len, int nthreads, bsg_book* out) 
         free_book(out);
         return BSG_ERR_INVALID_ARG;  // fewer records than the count
     }
-    // the reference reads exactly n records and ignores anything after them
-    size_t i = 0;
-    for (auto& p : parts)
-        for (const Rec& r : p) {
-            if (i == n) break;
-            store(out, i++, r);
-        }
+    // the reference reads exactly n records and ignores anything after
+    // them: each part is stored from its offset, the parts in parallel
+    std::vector<size_t> at(parts.size() + 1, 0);
+    for (size_t j = 0; j < parts.size(); ++j) at[j + 1] = at[j] + parts[j].size();
+    std::vector<std::thread> st;
+    for (size_t j = 0; j < parts.size(); ++j)
+        st.emplace_back([&, j] {
+            for (size_t k = 0; k < parts[j].size() && at[j] + k < n; ++k)
+                store(out, at[j] + k, parts[j][k]);
+        });
+    for (auto& t : st) t.join();
     return BSG_OK;
 }
 
 int bsg_read_parsec(const char* path, int nthreads, bsg_book* out) {
     if (!path || !out) return BSG_ERR_INVALID_ARG;
     std::memset(out, 0, sizeof(*out));
-    FILE* f = std::fopen(path, "rb");
-    if (!f) return BSG_ERR_INVALID_ARG;
-    std::fseek(f, 0, SEEK_END);
-    const long sz = std::ftell(f);
-    std::fseek(f, 0, SEEK_SET);
-    if (sz < 0) {
-        std::fclose(f);
+    const int fd = ::open(path, O_RDONLY);
+    if (fd < 0) return BSG_ERR_INVALID_ARG;
+    struct stat sb;
+    if (::fstat(fd, &sb) != 0 || sb.st_size < 0) {
+        ::close(fd);
         return BSG_ERR_INVALID_ARG;
     }
-    std::string buf((size_t)sz, '\0');
-    const size_t got = sz ? std::fread(&buf[0], 1, (size_t)sz, f) : 0;
-    std::fclose(f);
-    if (got != (size_t)sz) return BSG_ERR_INVALID_ARG;
-    return bsg_parse_parsec(buf.c_str(), buf.size(), nthreads, out);
+    const size_t sz = (size_t)sb.st_size;
+    // read in parallel, disjoint ranges with pread, into an uninitialised
+    // buffer ended by a NUL (for the strtof fallback)
+    std::unique_ptr<char[]> buf(new (std::nothrow) char[sz + 1]);
+    if (!buf) {
+        ::close(fd);
+        return BSG_ERR_OUT_OF_MEMORY;
+    }
+    const int T = clamp_threads(nthreads, sz, 8 << 20);
+    std::vector<int> ok(T, 1);
+    std::vector<std::thread> th;
+    for (int t = 0; t < T; ++t)
+        th.emplace_back([&, t] {
+            size_t a = sz * t / T;
+            const size_t b = sz * (t + 1) / T;
+            while (a < b) {
+                const ssize_t r = ::pread(fd, buf.get() + a, b - a, (off_t)a);
+                if (r <= 0) {
+                    if (r < 0 && errno == EINTR) continue;
+                    ok[t] = 0;
+                    return;
+                }
+                a += (size_t)r;
+            }
+        });
+    for (auto& x : th) x.join();
+    ::close(fd);
+    for (int v : ok)
+        if (!v) return BSG_ERR_INVALID_ARG;
+    buf[sz] = '\0';
+    return bsg_parse_parsec(buf.get(), sz, nthreads, out);
 }
 
 void bsg_book_free(bsg_book* b) { free_book(b); }

@@ -156,3 +156,49 @@ def test_parallel_io_equals_the_reference_sequential_io(tmp_path, oracle_lib):
     abi.write_parsec_prices(o1, prices, nthreads=4)
     oracle_lib.write_prices_fprintf(o2, prices)
     assert o1.read_bytes() == o2.read_bytes()
+
+
+def _tokens(rng, count):
+    """Decimal tokens of every shape the parser's fast path handles or must
+    hand to strtof: random floats and doubles at 1-20 significant digits,
+    float midpoints (ties in double, not always in decimal), integers, tiny
+    and huge magnitudes, signs, leading zeros, exponent forms."""
+    out = []
+    f = rng.standard_normal(count).astype(np.float32) * np.float32(10.0) ** rng.integers(-12, 12, count)
+    for i, x in enumerate(f):
+        prec = int(rng.integers(1, 21))
+        out.append(("%." + str(prec) + ("g" if i % 3 else "e")) % float(x))
+    # midpoints between adjacent floats, printed with enough digits to be exact
+    # in double and with digits that break the tie either way
+    base = (rng.random(count // 4) * 1e4).astype(np.float32)
+    nxt = np.nextafter(base, np.float32(np.inf))
+    mids = (base.astype(np.float64) + nxt.astype(np.float64)) / 2
+    for m in mids:
+        out += ["%.17g" % m, "%.25g" % m, "%.9g" % m, repr(float(m)) + "1", repr(float(m))[:-1]]
+    out += ["0", "-0", "-0.0", "000123.4500", "+7", ".5", "5.", "1e5", "1E-5", "2.5e+03",
+            "123456789012345678901", "0.000000000000000000012345", "3.4028235e38", "1e39",
+            "1.17549435e-38", "1e-45", "9007199254740993", "16777217", "0.1", "0.30000001"]
+    return out
+
+
+@pytest.mark.parametrize("threads", [1, 5])
+def test_parse_every_float_shape_like_strtof(threads):
+    rng = np.random.default_rng(77)
+    toks = _tokens(rng, 24000)
+    _libc.strtof.restype = ctypes.c_float
+    _libc.strtof.argtypes = [ctypes.c_char_p, ctypes.c_void_p]
+    want = np.array([_libc.strtof(t.encode(), None) for t in toks], dtype=np.float32)
+    # pack the tokens into records: 8 float fields (plus the type letter) per line
+    per = 8
+    n = len(toks) // per
+    lines = [str(n)]
+    for r in range(n):
+        t = toks[r * per:(r + 1) * per]
+        lines.append(" ".join(t[:6] + ["C"] + t[6:]))
+    book, dg = abi.parse_parsec(("\n".join(lines) + "\n").encode(), nthreads=threads)
+    got = np.stack([book.sptprice, book.strike, book.rate, np.zeros(n, np.float32),
+                    book.volatility, book.otime], axis=1)
+    ref = want[:n * per].reshape(n, per)
+    cols = [0, 1, 2, 4, 5]  # the fields the book keeps (divq is read and dropped)
+    assert np.array_equal(got[:, cols].view(np.uint32), ref[:, cols].view(np.uint32))
+    assert np.array_equal(dg.view(np.uint32), ref[:, 7].view(np.uint32))
