@@ -26,7 +26,13 @@
  * float on assignment, as in the reference.  exp() of a float argument in
  * the reference (a C++ translation unit) resolves to expf.
  */
-float bso_cndf_ref(float x)
+/* The reference's expf/logf (glibc), or, with cr set, exp/log correctly
+ * rounded to float (through double: exact to within double rounding) -- the
+ * rounding the GPU's reference-order mode targets. */
+static float ref_exp(float x, int cr) { return cr ? (float)exp((double)x) : expf(x); }
+static float ref_log(float x, int cr) { return cr ? (float)log((double)x) : logf(x); }
+
+static float cndf_ref(float x, int cr)
 {
     int sign = 0;
     if (x < 0.0) {                               /* :146-150 */
@@ -34,7 +40,7 @@ float bso_cndf_ref(float x)
         sign = 1;
     }
     const float xin = x;
-    const float e = expf(-0.5f * x * x);         /* :155 float product, expf */
+    const float e = ref_exp(-0.5f * x * x, cr);  /* :155 float product, expf */
     const float nprime = e * BSO_INV_SQRT_2PI;   /* :157 double, rounded */
 
     float k = 0.2316419 * xin;                   /* :159-161 three roundings */
@@ -61,11 +67,13 @@ float bso_cndf_ref(float x)
     return out;
 }
 
+float bso_cndf_ref(float x) { return cndf_ref(x, 0); }
+
 /* BlkSchlsEqEuroNoDiv, blackscholes.c:190-258 */
-float bso_price_ref(float s, float k, float r, float v, float t, int otype)
+static float price_ref(float s, float k, float r, float v, float t, int otype, int cr)
 {
     const float sqrt_t = sqrtf(t);               /* :226 */
-    const float lg = logf(s / k);                /* :228 */
+    const float lg = ref_log(s / k, cr);         /* :228 */
     float power = v * v;                         /* :233 */
     power = power * 0.5;                         /* :234 double, rounded */
     float d1 = r + power;                        /* :236-238 */
@@ -75,10 +83,10 @@ float bso_price_ref(float s, float k, float r, float v, float t, int otype)
     d1 = d1 / den;                               /* :241 */
     const float d2 = d1 - den;                   /* :242 */
 
-    const float n1 = bso_cndf_ref(d1);           /* :247-248 */
-    const float n2 = bso_cndf_ref(d2);
+    const float n1 = cndf_ref(d1, cr);           /* :247-248 */
+    const float n2 = cndf_ref(d2, cr);
 
-    const float fv = k * expf(-(r) * (t));       /* :250 */
+    const float fv = k * ref_exp(-(r) * (t), cr);  /* :250 */
     float price;
     if (otype == 0) {
         price = (s * n1) - (fv * n2);            /* :252 */
@@ -88,6 +96,16 @@ float bso_price_ref(float s, float k, float r, float v, float t, int otype)
         price = (fv * nn2) - (s * nn1);          /* :256 */
     }
     return price;
+}
+
+float bso_price_ref(float s, float k, float r, float v, float t, int otype)
+{
+    return price_ref(s, k, r, v, t, otype, 0);
+}
+
+float bso_price_ref_cr(float s, float k, float r, float v, float t, int otype)
+{
+    return price_ref(s, k, r, v, t, otype, 1);
 }
 
 /* The same polynomial and summation order in double throughout. */
@@ -133,6 +151,14 @@ void bso_price_ref_soa(size_t n, const float* s, const float* k, const float* r,
 {
     for (size_t i = 0; i < n; ++i)
         prices[i] = bso_price_ref(s[i], k[i], r[i], v[i], t[i], otype[i]);
+}
+
+void bso_price_ref_cr_soa(size_t n, const float* s, const float* k, const float* r,
+                          const float* v, const float* t, const int32_t* otype,
+                          float* prices)
+{
+    for (size_t i = 0; i < n; ++i)
+        prices[i] = bso_price_ref_cr(s[i], k[i], r[i], v[i], t[i], otype[i]);
 }
 
 void bso_price_fp64_soa(size_t n, const float* s, const float* k, const float* r,

@@ -33,6 +33,9 @@ extern "C" {
 float  bso_cndf_ref(float x);
 /* blackscholes.c:190-258 (timet is unused by the reference, so it is absent) */
 float  bso_price_ref(float s, float k, float r, float v, float t, int otype);
+/* The same operations with exp/log correctly rounded to float in place of
+ * glibc's expf/logf (the rounding the GPU's reference-order mode targets). */
+float  bso_price_ref_cr(float s, float k, float r, float v, float t, int otype);
 
 double bso_cndf_fp64(double x);
 double bso_price_fp64(double s, double k, double r, double v, double t, int otype);
@@ -43,6 +46,9 @@ double bso_d1_fp64(double s, double k, double r, double v, double t);
 void bso_price_ref_soa(size_t n, const float* s, const float* k, const float* r,
                        const float* v, const float* t, const int32_t* otype,
                        float* prices);
+void bso_price_ref_cr_soa(size_t n, const float* s, const float* k, const float* r,
+                          const float* v, const float* t, const int32_t* otype,
+                          float* prices);
 void bso_price_fp64_soa(size_t n, const float* s, const float* k, const float* r,
                         const float* v, const float* t, const int32_t* otype,
                         double* prices);

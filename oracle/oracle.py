@@ -57,6 +57,8 @@ def lib() -> ctypes.CDLL:
         L.bso_d1_fp64.argtypes = [ctypes.c_double] * 5
         L.bso_price_ref_soa.restype = None
         L.bso_price_ref_soa.argtypes = [ctypes.c_size_t] + [_P] * 7
+        L.bso_price_ref_cr_soa.restype = None
+        L.bso_price_ref_cr_soa.argtypes = [ctypes.c_size_t] + [_P] * 7
         L.bso_price_fp64_soa.restype = None
         L.bso_price_fp64_soa.argtypes = [ctypes.c_size_t] + [_P] * 7
         L.bso_price_fp64_soa_d.restype = None
@@ -101,6 +103,15 @@ def price_ref(book) -> np.ndarray:
     a = _arrs(book)
     out = np.empty(len(book), dtype=np.float32)
     lib().bso_price_ref_soa(len(book), *[_p(x) for x in a], _p(out))
+    return out
+
+
+def price_ref_cr(book) -> np.ndarray:
+    """The FP32 restatement with exp/log correctly rounded to float in place
+    of glibc's expf/logf: the rounding the reference-order GPU mode targets."""
+    a = _arrs(book)
+    out = np.empty(len(book), dtype=np.float32)
+    lib().bso_price_ref_cr_soa(len(book), *[_p(x) for x in a], _p(out))
     return out
 
 

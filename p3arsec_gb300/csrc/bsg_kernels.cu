@@ -152,7 +152,9 @@ __device__ __forceinline__ void price_groups(const SoA& a, int64_t g0, int64_t g
 // stores, so a pass still completes after the one before it.  Both
 // instructions are no-ops for a launch without the PDL attribute.
 // Registers: one-group shapes (VPT = 1) are held to 64 per thread (1024
-// threads per SM, no spills); more groups per thread need up to 128.
+// threads per SM, no spills); more groups per thread need up to 128.  The
+// reference-order libm mode (compute-bound, float-float exp/log) always runs
+// 256-thread blocks, four per SM (59 registers, no spills).
 __device__ __forceinline__ void pdl_trigger() {
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
@@ -161,7 +163,9 @@ __device__ __forceinline__ void pdl_wait() {
 }
 
 template <int M, int W, int VPT, int LP>
-__global__ void __launch_bounds__(512, VPT == 1 ? 2 : 1) map_vec_kernel(SoA a, int64_t n) {
+__global__ void __launch_bounds__(M == MODE_LIBM_REF ? 256 : 512,
+                                  M == MODE_LIBM_REF ? 4 : (VPT == 1 ? 2 : 1))
+    map_vec_kernel(SoA a, int64_t n) {
     pdl_trigger();
     const unsigned long long pol = lp_evict_first(LP) ? evict_first_policy() : 0ull;
     const int64_t ngroups = n / W;
@@ -409,8 +413,18 @@ static cudaError_t launch_map_bulk(const SoA& a, int64_t n, const MapCfg& cfg, i
 }
 
 template <int M>
-static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg,
+static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg_in,
                                    int sm_count, cudaStream_t st) {
+    MapCfg cfg = cfg_in;
+    if constexpr (M == MODE_LIBM_REF) {
+        // compute-bound (float-float exp/log): 128-bit loads and one
+        // 256-thread block per tile (four resident per SM), whatever shape
+        // the memory-bound tuning chose
+        cfg.load_path = 0;
+        cfg.vpt = 1;
+        cfg.blocks_per_sm = 0;
+        if (cfg.block > 256) cfg.block = 256;
+    }
     const int block = cfg.block;
     if (!map_vectorizable(a, cfg)) {
         int64_t grid = (n + 255) / 256;
@@ -475,8 +489,9 @@ static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg,
             default: return cudaErrorInvalidValue;
         }
     } else {
-        // reference-order paths are validation variants: one shape.
-        if (lp_v8(cfg.load_path)) BSG_LAUNCH(8, 1, 2);
+        // reference-order paths are validation variants: one shape each.
+        if constexpr (M == MODE_LIBM_REF) BSG_LAUNCH(4, 1, 0);
+        else if (lp_v8(cfg.load_path)) BSG_LAUNCH(8, 1, 2);
         else BSG_LAUNCH(4, 1, 0);
     }
 #undef BSG_LAUNCH
@@ -568,9 +583,10 @@ __device__ __forceinline__ void price_range(const SoA& pool, uint64_t b, uint64_
 // Persistent kernel: each block takes the next tile from the device work
 // counter, maps it to its segment by binary search over the tile prefix and
 // prices it.  No block ever waits on another; the loop ends when the counter
-// passes the last tile.
+// passes the last tile.  (Four blocks per SM hold the registers to 64; the
+// libm mode's float-float exp/log get up to 128.)
 template <int M, int W>
-__global__ void __launch_bounds__(kBatchBlock, 4) batch_kernel(
+__global__ void __launch_bounds__(kBatchBlock, M == MODE_LIBM_REF ? 2 : 4) batch_kernel(
     SoA pool, const uint64_t* __restrict__ seg_off, const uint64_t* __restrict__ seg_len,
     const uint64_t* __restrict__ tile_prefix, int nseg, uint64_t ntiles, uint64_t topt,
     unsigned long long* cursor) {
@@ -632,8 +648,9 @@ cudaError_t launch_batch(const SoA& pool, const uint64_t* seg_off,
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     lc.attrs = attr;
     lc.numAttrs = pdl ? 1 : 0;
-    // 256-bit loads need every pool array 32-byte aligned
-    const bool w8 = map_vectorizable(pool, MapCfg{1, kBatchBlock, 0, 2, 0});
+    // 256-bit loads need every pool array 32-byte aligned; the libm mode
+    // keeps 128-bit loads (fewer registers: it is compute-bound)
+    const bool w8 = mode != MODE_LIBM_REF && map_vectorizable(pool, MapCfg{1, kBatchBlock, 0, 2, 0});
 #define BSG_BATCH(M_) \
     (w8 ? cudaLaunchKernelEx(&lc, batch_kernel<M_, 8>, pool, seg_off, seg_len, tile_prefix, nseg, \
                              ntiles, tile_opts, cursor) \

@@ -8,9 +8,11 @@
 //                   where their error cancels, error-free transformations
 //                   where it does not (see the notes on each step).
 //   price_sfu_ref   the reference's operation order with SFU intrinsics.
-//   price_libm_ref  the reference's operation order with CUDA's accurate
-//                   expf/logf, IEEE division and square root, and the
-//                   reference's double-literal products emulated in FP32.
+//   price_libm_ref  the reference's operation order with correctly rounded
+//                   exp/log (float-float, bsg_crmath.h), IEEE division and
+//                   square root, and the reference's double-literal
+//                   products emulated in FP32: the reference's rounding
+//                   wherever glibc's expf/logf round correctly.
 //   price_fp64      the same formula in double (validation oracle).
 //
 // Every function here is branch-free per option apart from selects, and uses
@@ -20,6 +22,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "bsg_crmath.h"
 #include "bsg_internal.h"
 
 namespace bsg {
@@ -342,9 +345,11 @@ __device__ __forceinline__ float price_sfu_ref(float s, float k, float r, float 
 // `float = float * <double literal>` lines evaluate (to within the rare
 // double-rounding case).  An infinite x gives c.hi * x, the double product's
 // value (c.hi x + c.lo x would be inf - inf when c.lo has the other sign).
+__device__ __forceinline__ float dmul_finite(float x, FF c) {
+    return __fmaf_rn(c.hi, x, __fmul_rn(c.lo, x));
+}
 __device__ __forceinline__ float dmul(float x, FF c) {
-    const float p = __fmaf_rn(c.hi, x, __fmul_rn(c.lo, x));
-    return isinf(x) ? __fmul_rn(c.hi, x) : p;
+    return isinf(x) ? __fmul_rn(c.hi, x) : dmul_finite(x, c);
 }
 
 __device__ __forceinline__ float cndf_libm_ref(float x) {
@@ -353,20 +358,22 @@ __device__ __forceinline__ float cndf_libm_ref(float x) {
     constexpr FF isp = split(BSG_INV_SQRT_2PI);
     const bool neg = x < 0.0f;                                   // :146-150
     x = neg ? -x : x;
-    const float e = expf(__fmul_rn(__fmul_rn(-0.5f, x), x));     // :155
-    const float np = dmul(e, isp);                               // :157
+    // x = |d1| may be infinite (v sqrt(t) = 0); e and k = 1 / (1 + x c0)
+    // are always finite (in [0, 1]), so only x c0 needs dmul's inf case
+    const float e = bsg_cr::exp(__fmul_rn(__fmul_rn(-0.5f, x), x));  // :155
+    const float np = dmul_finite(e, isp);                        // :157
     float k = dmul(x, c0);                                       // :159
     k = __fadd_rn(1.0f, k);                                      // :160
     k = __fdiv_rn(1.0f, k);                                      // :161
     const float k2 = __fmul_rn(k, k), k3 = __fmul_rn(k2, k);     // :162-165
     const float k4 = __fmul_rn(k3, k), k5 = __fmul_rn(k4, k);
-    float l1 = dmul(k, c1);                                      // :167
-    float l2 = dmul(k2, c2);                                     // :168
-    float l3 = dmul(k3, c3);                                     // :169
+    float l1 = dmul_finite(k, c1);                               // :167
+    float l2 = dmul_finite(k2, c2);                              // :168
+    float l3 = dmul_finite(k3, c3);                              // :169
     l2 = __fadd_rn(l2, l3);
-    l3 = dmul(k4, c4);
+    l3 = dmul_finite(k4, c4);
     l2 = __fadd_rn(l2, l3);
-    l3 = dmul(k5, c5);
+    l3 = dmul_finite(k5, c5);
     l2 = __fadd_rn(l2, l3);                                      // :174
     l1 = __fadd_rn(l2, l1);                                      // :176
     float out = __fmul_rn(l1, np);                               // :177
@@ -377,7 +384,7 @@ __device__ __forceinline__ float cndf_libm_ref(float x) {
 __device__ __forceinline__ float price_libm_ref(float s, float k, float r, float v,
                                                 float t, int otype) {
     const float sq = __fsqrt_rn(t);                              // :226
-    const float lg = logf(__fdiv_rn(s, k));                      // :228
+    const float lg = bsg_cr::log(__fdiv_rn(s, k));               // :228
     float pw = __fmul_rn(v, v);                                  // :233
     pw = __fmul_rn(pw, 0.5f);                                    // :234 (exact)
     float d1 = __fadd_rn(r, pw);                                 // :236
@@ -387,10 +394,152 @@ __device__ __forceinline__ float price_libm_ref(float s, float k, float r, float
     d1 = __fdiv_rn(d1, den);                                     // :241
     const float d2 = __fsub_rn(d1, den);                         // :242
     const float n1 = cndf_libm_ref(d1), n2 = cndf_libm_ref(d2);
-    const float fv = __fmul_rn(k, expf(__fmul_rn(-r, t)));       // :250
+    const float fv = __fmul_rn(k, bsg_cr::exp(__fmul_rn(-r, t)));  // :250
     if (otype == 0) return __fsub_rn(__fmul_rn(s, n1), __fmul_rn(fv, n2));
     const float nn1 = __fsub_rn(1.0f, n1), nn2 = __fsub_rn(1.0f, n2);
     return __fsub_rn(__fmul_rn(fv, nn2), __fmul_rn(s, nn1));     // :256
+}
+
+// Two options at a time: the operations of cndf_libm_ref / price_libm_ref
+// and of bsg_cr::exp / bsg_cr::log, each as one packed f32x2 operation
+// where the scalar code has a float operation (componentwise the same
+// rounding: the same bits), per lane where it has a division, a square
+// root, integer work or a table load -- and per lane where the reference
+// rounds a product and then adds it: the toolchain fuses an f32x2 multiply
+// into the f32x2 add or subtract that is its only use (even from inline
+// PTX mul.rn.f32x2 / add.rn.f32x2, and under -fmad=false), which would skip
+// that rounding.
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return add2(a, neg2(b)); }
+struct FF2 { float2 hi, lo; };
+__device__ __forceinline__ FF2 two_sum2(float2 a, float2 b) {
+    const float2 s = add2(a, b);
+    const float2 bb = sub2(s, a);
+    return {s, add2(sub2(a, sub2(s, bb)), sub2(b, bb))};
+}
+__device__ __forceinline__ FF2 fast_two_sum2(float2 a, float2 b) {
+    const float2 s = add2(a, b);
+    return {s, sub2(b, sub2(s, a))};
+}
+__device__ __forceinline__ FF2 two_prod2(float2 a, float2 b) {
+    const float2 p = mul2(a, b);
+    return {p, fma2(a, b, neg2(p))};
+}
+__device__ __forceinline__ bool cr_exp_in_range(float x) { return x >= -87.0f && x <= 88.5f; }
+__device__ __forceinline__ bool cr_log_in_range(float x) {
+    return x >= 1.17549435e-38f && x <= 3.40282347e38f;
+}
+
+__device__ __forceinline__ float2 cr_exp2(float2 x) {
+    if (!(cr_exp_in_range(x.x) && cr_exp_in_range(x.y)))
+        return make_float2(bsg_cr::exp(x.x), bsg_cr::exp(x.y));
+    const float2 sh = fma2(x, f2(BSG_CR_INV_L), f2(bsg_cr::kShifter));
+    const float2 nf = sub2(sh, f2(bsg_cr::kShifter));
+    const int n0 = (int)(__float_as_uint(sh.x) - bsg_cr::kShifterBits);
+    const int n1 = (int)(__float_as_uint(sh.y) - bsg_cr::kShifterBits);
+    const float2 r1 = fma2(neg2(nf), f2(BSG_CR_L1), x);
+    const FF2 p = two_prod2(nf, f2(BSG_CR_L2));
+    const FF2 rs = two_sum2(r1, neg2(p.hi));
+    const float2 rh = rs.hi;
+    const float2 rl = fma2(neg2(nf), f2(BSG_CR_L3), sub2(rs.lo, p.lo));
+    const FF2 s2 = two_prod2(rh, rh);
+    float2 c = fma2(rh, f2(1.0f / 120.0f), f2(1.0f / 24.0f));
+    c = fma2(rh, c, f2(1.0f / 6.0f));
+    c = mul2(rh, c);
+    const FF2 q = fast_two_sum2(rh, mul2(s2.hi, f2(0.5f)));
+    const float2 ql =
+        add2(q.lo, add2(rl, fma2(s2.lo, f2(0.5f), fma2(rh, rl, mul2(s2.hi, c)))));
+    const bsg_cr::F2 t0 = bsg_cr::exp_tab(n0 & 31), t1 = bsg_cr::exp_tab(n1 & 31);
+    const float2 thi = make_float2(t0.hi, t1.hi), tlo = make_float2(t0.lo, t1.lo);
+    const FF2 tq = two_prod2(thi, q.hi);
+    const FF2 sm = fast_two_sum2(thi, tq.hi);
+    const float2 lo = add2(sm.lo, add2(tq.lo, add2(tlo, fma2(thi, ql, mul2(tlo, q.hi)))));
+    const float2 y = add2(sm.hi, lo);
+    return mul2(y, make_float2(__uint_as_float((uint32_t)((n0 >> 5) + 127) << 23),
+                               __uint_as_float((uint32_t)((n1 >> 5) + 127) << 23)));
+}
+
+__device__ __forceinline__ float2 cr_log2(float2 x) {
+    if (!(cr_log_in_range(x.x) && cr_log_in_range(x.y)))
+        return make_float2(bsg_cr::log(x.x), bsg_cr::log(x.y));
+    const uint32_t u0 = __float_as_uint(x.x), u1 = __float_as_uint(x.y);
+    const uint32_t i0 = (u0 >> 15) & 0xFFu, i1 = (u1 >> 15) & 0xFFu;
+    const int e0 = (int)(u0 >> 23) - 127 + (int)(i0 >> 7);
+    const int e1 = (int)(u1 >> 23) - 127 + (int)(i1 >> 7);
+    const float2 m = make_float2(
+        __uint_as_float((u0 & 0x7FFFFFu) | (i0 >= 128 ? 0x3F000000u : 0x3F800000u)),
+        __uint_as_float((u1 & 0x7FFFFFu) | (i1 >= 128 ? 0x3F000000u : 0x3F800000u)));
+    const bsg_cr::LogEntry g0 = bsg_cr::log_tab((int)i0), g1 = bsg_cr::log_tab((int)i1);
+    const float2 r = fma2(m, make_float2(g0.c, g1.c), f2(-1.0f));
+    const FF2 s2 = two_prod2(r, r);
+    float2 c = fma2(r, f2(0.2f), f2(-0.25f));
+    c = fma2(r, c, f2(1.0f / 3.0f));
+    c = mul2(mul2(s2.hi, r), c);
+    const FF2 a = fast_two_sum2(r, mul2(s2.hi, f2(-0.5f)));
+    const float2 alo = add2(a.lo, fma2(s2.lo, f2(-0.5f), c));
+    const float2 ef = sub2(make_float2(__uint_as_float(bsg_cr::kShifterBits + (uint32_t)e0),
+                                       __uint_as_float(bsg_cr::kShifterBits + (uint32_t)e1)),
+                           f2(bsg_cr::kShifter));
+    const FF2 em = two_prod2(ef, f2(BSG_CR_LN2M));
+    const FF2 s1 = two_sum2(mul2(ef, f2(BSG_CR_LN2H)), make_float2(g0.hi, g1.hi));
+    const FF2 s2s = two_sum2(s1.hi, a.hi);
+    const FF2 s3 = two_sum2(s2s.hi, em.hi);
+    const float2 lo = add2(add2(add2(s1.lo, s2s.lo), s3.lo),
+                           add2(add2(make_float2(g0.lo, g1.lo), alo),
+                                fma2(ef, f2(BSG_CR_LN2L), em.lo)));
+    return add2(s3.hi, lo);
+}
+
+__device__ __forceinline__ float2 dmul_finite2(float2 x, FF c) {
+    return fma2(f2(c.hi), x, mul2(f2(c.lo), x));
+}
+
+__device__ __forceinline__ float2 cndf_libm_ref2(float2 xin) {
+    constexpr FF c0 = split(BSG_C0), c1 = split(BSG_C1), c2 = split(BSG_C2);
+    constexpr FF c3 = split(BSG_C3), c4 = split(BSG_C4), c5 = split(BSG_C5);
+    constexpr FF isp = split(BSG_INV_SQRT_2PI);
+    const bool neg0 = xin.x < 0.0f, neg1 = xin.y < 0.0f;
+    const float2 x = make_float2(neg0 ? -xin.x : xin.x, neg1 ? -xin.y : xin.y);
+    const float2 e = cr_exp2(mul2(mul2(f2(-0.5f), x), x));
+    const float2 np = dmul_finite2(e, isp);
+    float2 k = make_float2(dmul(x.x, c0), dmul(x.y, c0));
+    k = add2(f2(1.0f), k);
+    k = make_float2(__fdiv_rn(1.0f, k.x), __fdiv_rn(1.0f, k.y));
+    const float2 k2 = mul2(k, k), k3 = mul2(k2, k);
+    const float2 k4 = mul2(k3, k), k5 = mul2(k4, k);
+    float2 l1 = dmul_finite2(k, c1);
+    float2 l2 = dmul_finite2(k2, c2);
+    float2 l3 = dmul_finite2(k3, c3);
+    l2 = add2(l2, l3);
+    l3 = dmul_finite2(k4, c4);
+    l2 = add2(l2, l3);
+    l3 = dmul_finite2(k5, c5);
+    l2 = add2(l2, l3);
+    l1 = add2(l2, l1);
+    const float2 out = make_float2(__fsub_rn(1.0f, __fmul_rn(l1.x, np.x)),
+                                   __fsub_rn(1.0f, __fmul_rn(l1.y, np.y)));
+    const float2 refl = sub2(f2(1.0f), out);
+    return make_float2(neg0 ? refl.x : out.x, neg1 ? refl.y : out.y);
+}
+
+__device__ __forceinline__ float2 price_libm_ref2(float2 s, float2 k, float2 r, float2 v,
+                                                  float2 t, int ot0, int ot1) {
+    const float2 sq = make_float2(__fsqrt_rn(t.x), __fsqrt_rn(t.y));
+    const float2 lg = cr_log2(make_float2(__fdiv_rn(s.x, k.x), __fdiv_rn(s.y, k.y)));
+    float2 pw = mul2(v, v);
+    pw = mul2(pw, f2(0.5f));
+    float2 d1 = add2(r, pw);
+    d1 = make_float2(__fadd_rn(__fmul_rn(d1.x, t.x), lg.x), __fadd_rn(__fmul_rn(d1.y, t.y), lg.y));
+    const float2 den = mul2(v, sq);
+    d1 = make_float2(__fdiv_rn(d1.x, den.x), __fdiv_rn(d1.y, den.y));
+    const float2 d2 = sub2(d1, den);
+    const float2 n1 = cndf_libm_ref2(d1), n2 = cndf_libm_ref2(d2);
+    const float2 fv = mul2(k, cr_exp2(mul2(neg2(r), t)));
+    const float2 nn1 = sub2(f2(1.0f), n1), nn2 = sub2(f2(1.0f), n2);
+    const float p0 = ot0 == 0 ? __fsub_rn(__fmul_rn(s.x, n1.x), __fmul_rn(fv.x, n2.x))
+                              : __fsub_rn(__fmul_rn(fv.x, nn2.x), __fmul_rn(s.x, nn1.x));
+    const float p1 = ot1 == 0 ? __fsub_rn(__fmul_rn(s.y, n1.y), __fmul_rn(fv.y, n2.y))
+                              : __fsub_rn(__fmul_rn(fv.y, nn2.y), __fmul_rn(s.y, nn1.y));
+    return make_float2(p0, p1);
 }
 
 // ------------------------------------------------------------------- FP64
@@ -451,6 +600,14 @@ __device__ __forceinline__ float4 price4(float4 s, float4 k, float4 r, float4 v,
         const float2 b = price_fast2(make_float2(s.z, s.w), make_float2(k.z, k.w),
                                      make_float2(r.z, r.w), make_float2(v.z, v.w),
                                      make_float2(t.z, t.w), ot.z, ot.w);
+        return make_float4(a.x, a.y, b.x, b.y);
+    } else if constexpr (M == MODE_LIBM_REF) {
+        const float2 a = price_libm_ref2(make_float2(s.x, s.y), make_float2(k.x, k.y),
+                                         make_float2(r.x, r.y), make_float2(v.x, v.y),
+                                         make_float2(t.x, t.y), ot.x, ot.y);
+        const float2 b = price_libm_ref2(make_float2(s.z, s.w), make_float2(k.z, k.w),
+                                         make_float2(r.z, r.w), make_float2(v.z, v.w),
+                                         make_float2(t.z, t.w), ot.z, ot.w);
         return make_float4(a.x, a.y, b.x, b.y);
     } else {
         return make_float4(price<M>(s.x, k.x, r.x, v.x, t.x, ot.x),
