@@ -41,7 +41,7 @@ SEED = 20241203
 # between passes, so traffic is not proportional to the options: sizes and
 # shapes not captured report null.
 NCU_DRAM_BYTES_PER_PASS = {(1, 10_000_000): 206.0e6, (2, 10_000_000): 266.1e6,
-                           (6, 10_000_000): 206.9e6}
+                           (6, 10_000_000): 206.9e6, (7, 10_000_000): 228.9e6}
 NCU_PROFILE = "profiles/map_fast_10M.md"
 
 

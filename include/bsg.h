@@ -392,7 +392,11 @@ typedef struct bsg_tune {
                                ring of 3 x 48 KB (1 CTA per SM), 4 x 24 KB
                                (2 per SM) or 3 x 24 KB (3 per SM); block and
                                grid are then fixed,
-                           6 = LDG.256 evict-first (vec_per_thread 1 or 2) */
+                           6 = LDG.256 evict-first (vec_per_thread 1 or 2),
+                           7 = LDG.256 and STG.256 with the book's first
+                               options (15/32 of the L2 at 28 bytes each)
+                               evict-last, the rest evict-first: that
+                               prefix stays in L2 across passes */
     int pdl;            /* 1 = programmatic dependent launch between passes */
 } bsg_tune;
 

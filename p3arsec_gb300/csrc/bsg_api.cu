@@ -1063,7 +1063,7 @@ static bool tune_valid(const bsg_tune* t) {
                         (t->vec_per_thread == 4 && t->load_path < 2);
     const bool blk_ok = t->block == 128 || t->block == 256 || t->block == 512;
     return vpt_ok && blk_ok && t->blocks_per_sm >= 0 && t->blocks_per_sm <= 64 &&
-           t->load_path >= 0 && t->load_path <= 6 && (t->pdl == 0 || t->pdl == 1);
+           t->load_path >= 0 && t->load_path <= 7 && (t->pdl == 0 || t->pdl == 1);
 }
 
 int bsg_set_tune(bsg_ctx* c, const bsg_tune* t) {
@@ -1174,7 +1174,7 @@ extern "C" int bsg_autotune(bsg_ctx* c, size_t n, bsg_tune* out) {
     };
     // sweep: every shape for 5 passes
     std::vector<std::pair<float, bsg_tune>> timed;
-    for (int lp : {0, 1, 2, 6})
+    for (int lp : {0, 1, 2, 6, 7})
         for (int vpt : {1, 2, 4})
             for (int block : {128, 256, 512})
                 for (int bps : {0, 2, 4, 8})

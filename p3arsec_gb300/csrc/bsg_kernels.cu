@@ -27,6 +27,11 @@ __device__ __forceinline__ unsigned long long evict_first_policy() {
     asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
     return pol;
 }
+__device__ __forceinline__ unsigned long long evict_last_policy() {
+    unsigned long long pol;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
 
 template <int W>
 struct Raw {
@@ -35,9 +40,14 @@ struct Raw {
 
 // Load paths of the vector kernel: LP 0/2: ld.global.nc.L1::no_allocate
 // (v4 / v8); LP 1 / 6: the same v4 / v8 loads with an L2 evict_first cache
-// policy.
+// policy; LP 7: v8 loads and stores of a resident prefix of the book (the
+// first `gres` groups, sized to about half the L2) with an evict_last
+// policy, the rest evict_first -- the prefix then stays in L2 from pass to
+// pass while the rest streams through.
+__host__ __device__ constexpr bool lp_resident(int lp) { return lp == 7; }
+__host__ __device__ constexpr bool lp_hinted(int lp) { return lp == 1 || lp == 6 || lp == 7; }
 __host__ __device__ constexpr bool lp_evict_first(int lp) { return lp == 1 || lp == 6; }
-__host__ __device__ constexpr bool lp_v8(int lp) { return lp == 2 || lp == 6; }
+__host__ __device__ constexpr bool lp_v8(int lp) { return lp == 2 || lp == 6 || lp == 7; }
 
 template <int W, int LP>
 __device__ __forceinline__ Raw<W> ld_group(const void* p, unsigned long long pol) {
@@ -53,7 +63,7 @@ __device__ __forceinline__ Raw<W> ld_group(const void* p, unsigned long long pol
                 : "=r"(r.v[0]), "=r"(r.v[1]), "=r"(r.v[2]), "=r"(r.v[3])
                 : "l"(p));
         }
-    } else if constexpr (lp_evict_first(LP)) {
+    } else if constexpr (lp_hinted(LP)) {
         asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8], %9;"
             : "=r"(r.v[0]), "=r"(r.v[1]), "=r"(r.v[2]), "=r"(r.v[3]),
               "=r"(r.v[4]), "=r"(r.v[5]), "=r"(r.v[6]), "=r"(r.v[7])
@@ -68,9 +78,15 @@ __device__ __forceinline__ Raw<W> ld_group(const void* p, unsigned long long pol
     return r;
 }
 
-template <int W>
-__device__ __forceinline__ void st_group(float* p, const float (&x)[W]) {
-    if constexpr (W == 4) {
+template <int W, int LP>
+__device__ __forceinline__ void st_group(float* p, const float (&x)[W], unsigned long long pol) {
+    if constexpr (W == 8 && lp_resident(LP)) {
+        asm volatile("st.global.L2::cache_hint.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8}, %9;"
+                     :: "l"(p), "f"(x[0]), "f"(x[1]), "f"(x[2]), "f"(x[3]),
+                        "f"(x[4]), "f"(x[5]), "f"(x[6]), "f"(x[7]), "l"(pol)
+                     : "memory");
+    } else if constexpr (W == 4) {
+        (void)pol;
         asm volatile("st.global.cs.v4.f32 [%0], {%1,%2,%3,%4};"
                      :: "l"(p), "f"(x[0]), "f"(x[1]), "f"(x[2]), "f"(x[3])
                      : "memory");
@@ -91,10 +107,12 @@ __device__ __forceinline__ void price_scalar(const SoA& a, int64_t i) {
 
 // Prices vector groups [g0, g1) (group = W options) of one block's range:
 // each thread loads VPT groups (stride blockDim.x) of all six arrays, then
-// computes and stores them.
+// computes and stores them.  pol is the L2 policy of the hinted load paths;
+// for LP 7, groups below gres use pol_res instead.
 template <int M, int W, int VPT, int LP>
 __device__ __forceinline__ void price_groups(const SoA& a, int64_t g0, int64_t g1,
-                                             unsigned long long pol) {
+                                             unsigned long long pol,
+                                             unsigned long long pol_res, int64_t gres) {
     const int64_t bd = blockDim.x;
     for (int64_t base = g0; base < g1; base += bd * VPT) {
         Raw<W> S[VPT], K[VPT], R[VPT], V[VPT], T[VPT], O[VPT];
@@ -103,12 +121,13 @@ __device__ __forceinline__ void price_groups(const SoA& a, int64_t g0, int64_t g
             const int64_t g = base + threadIdx.x + j * bd;
             if (g < g1) {
                 const int64_t o = g * W;
-                S[j] = ld_group<W, LP>(a.s + o, pol);
-                K[j] = ld_group<W, LP>(a.k + o, pol);
-                R[j] = ld_group<W, LP>(a.r + o, pol);
-                V[j] = ld_group<W, LP>(a.v + o, pol);
-                T[j] = ld_group<W, LP>(a.t + o, pol);
-                O[j] = ld_group<W, LP>(a.ot + o, pol);
+                const unsigned long long pl = (lp_resident(LP) && g < gres) ? pol_res : pol;
+                S[j] = ld_group<W, LP>(a.s + o, pl);
+                K[j] = ld_group<W, LP>(a.k + o, pl);
+                R[j] = ld_group<W, LP>(a.r + o, pl);
+                V[j] = ld_group<W, LP>(a.v + o, pl);
+                T[j] = ld_group<W, LP>(a.t + o, pl);
+                O[j] = ld_group<W, LP>(a.ot + o, pl);
             }
         }
 #pragma unroll
@@ -136,7 +155,8 @@ __device__ __forceinline__ void price_groups(const SoA& a, int64_t g0, int64_t g
                     p[e + 2] = q.z;
                     p[e + 3] = q.w;
                 }
-                st_group<W>(a.out + g * W, p);
+                const unsigned long long pst = (lp_resident(LP) && g < gres) ? pol_res : pol;
+                st_group<W, LP>(a.out + g * W, p, pst);
             }
         }
     }
@@ -165,14 +185,16 @@ __device__ __forceinline__ void pdl_wait() {
 template <int M, int W, int VPT, int LP>
 __global__ void __launch_bounds__(M == MODE_LIBM_REF ? 256 : 512,
                                   M == MODE_LIBM_REF ? 4 : (VPT == 1 ? 2 : 1))
-    map_vec_kernel(SoA a, int64_t n) {
+    map_vec_kernel(SoA a, int64_t n, int64_t gres) {
     pdl_trigger();
-    const unsigned long long pol = lp_evict_first(LP) ? evict_first_policy() : 0ull;
+    const unsigned long long pol =
+        (lp_evict_first(LP) || lp_resident(LP)) ? evict_first_policy() : 0ull;
+    const unsigned long long pol_res = lp_resident(LP) ? evict_last_policy() : 0ull;
     const int64_t ngroups = n / W;
     const int64_t tile = (int64_t)blockDim.x * VPT;
     for (int64_t t0 = (int64_t)blockIdx.x * tile; t0 < ngroups; t0 += (int64_t)gridDim.x * tile) {
         const int64_t t1 = (t0 + tile < ngroups) ? t0 + tile : ngroups;
-        price_groups<M, W, VPT, LP>(a, t0, t1, pol);
+        price_groups<M, W, VPT, LP>(a, t0, t1, pol, pol_res, gres);
     }
     if (blockIdx.x == 0) {
         const int64_t i = ngroups * W + threadIdx.x;
@@ -336,7 +358,7 @@ __global__ void __launch_bounds__(kBulkThreads) map_bulk_kernel(SoA a, int64_t n
         }
 #pragma unroll
         for (int h = 0; h < OPT / 4; ++h)
-            st_group<4>(a.out + tile * TILE + 1024 * h + 4 * threadIdx.x, p[h]);
+            st_group<4, 0>(a.out + tile * TILE + 1024 * h + 4 * threadIdx.x, p[h], 0ull);
     }
     if (k < mine) {
         // timed out: record it, let this CTA's copies in flight land (bounded)
@@ -412,6 +434,21 @@ static cudaError_t launch_map_bulk(const SoA& a, int64_t n, const MapCfg& cfg, i
     return cudaLaunchKernelEx(&lc, map_bulk_kernel<M, OPT, STAGES>, a, n, wait_ns, tx_extra);
 }
 
+// The current device's L2 size in bytes (0 if unknown), cached per device.
+static int64_t device_l2_bytes() {
+    static std::atomic<int64_t> cache[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+    int64_t v = cache[dev].load(std::memory_order_relaxed);
+    if (v == 0) {
+        int b = 0;
+        if (cudaDeviceGetAttribute(&b, cudaDevAttrL2CacheSize, dev) != cudaSuccess) return 0;
+        v = b;
+        cache[dev].store(v, std::memory_order_relaxed);
+    }
+    return v;
+}
+
 template <int M>
 static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg_in,
                                    int sm_count, cudaStream_t st) {
@@ -451,6 +488,13 @@ static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg_in
     }
     const int W = lp_v8(cfg.load_path) ? 8 : 4;
     const int64_t ngroups = n / W;
+    // LP 7: the first gres groups (15/32 of the L2 in inputs and prices,
+    // 28 bytes an option) are kept resident across passes
+    int64_t gres = 0;
+    if (lp_resident(cfg.load_path)) {
+        gres = device_l2_bytes() * 15 / 32 / (28 * W);
+        if (gres > ngroups) gres = ngroups;
+    }
     const int64_t tile = (int64_t)block * cfg.vpt;
     int64_t ntiles = (ngroups + tile - 1) / tile;
     int64_t grid = ntiles;
@@ -473,7 +517,7 @@ static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg_in
     lc.attrs = attr;
     lc.numAttrs = cfg.pdl ? 1 : 0;
     cudaError_t le = cudaSuccess;
-#define BSG_LAUNCH(W_, V_, L_) le = cudaLaunchKernelEx(&lc, map_vec_kernel<M, W_, V_, L_>, a, n)
+#define BSG_LAUNCH(W_, V_, L_) le = cudaLaunchKernelEx(&lc, map_vec_kernel<M, W_, V_, L_>, a, n, gres)
     if constexpr (M == MODE_FAST) {
         switch (cfg.load_path * 10 + cfg.vpt) {
             case 1: BSG_LAUNCH(4, 1, 0); break;
@@ -486,6 +530,8 @@ static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg_in
             case 22: BSG_LAUNCH(8, 2, 2); break;
             case 61: BSG_LAUNCH(8, 1, 6); break;
             case 62: BSG_LAUNCH(8, 2, 6); break;
+            case 71: BSG_LAUNCH(8, 1, 7); break;
+            case 72: BSG_LAUNCH(8, 2, 7); break;
             default: return cudaErrorInvalidValue;
         }
     } else {
@@ -573,9 +619,9 @@ __device__ __forceinline__ void price_range(const SoA& pool, uint64_t b, uint64_
     const uint64_t i_head = b + threadIdx.x;
     if (i_head < head_end) price_scalar<M>(pool, (int64_t)i_head);
     if constexpr (W == 8)
-        price_groups<M, 8, 1, 2>(pool, (int64_t)(head_end / 8), (int64_t)(body_end / 8), 0ull);
+        price_groups<M, 8, 1, 2>(pool, (int64_t)(head_end / 8), (int64_t)(body_end / 8), 0ull, 0ull, 0);
     else
-        price_groups<M, 4, kBatchVpt, 0>(pool, (int64_t)(head_end / 4), (int64_t)(body_end / 4), 0ull);
+        price_groups<M, 4, kBatchVpt, 0>(pool, (int64_t)(head_end / 4), (int64_t)(body_end / 4), 0ull, 0ull, 0);
     const uint64_t i_tail = body_end + threadIdx.x;
     if (i_tail < e) price_scalar<M>(pool, (int64_t)i_tail);
 }

@@ -155,7 +155,7 @@ def test_all_tunings_give_identical_bits(gpu_ctx):
     base = gpu_ctx.price_book(book)
     saved = gpu_ctx.get_tune()
     try:
-        for lp in (0, 1, 2, 3, 4, 5, 6):
+        for lp in (0, 1, 2, 3, 4, 5, 6, 7):
             for vpt in (1, 2, 4):
                 if lp >= 2 and vpt == 4:
                     continue
@@ -164,6 +164,23 @@ def test_all_tunings_give_identical_bits(gpu_ctx):
                         gpu_ctx.set_tune(vpt, block, bps, lp, pdl)
                         got = gpu_ctx.price_book(book, num_runs=3)
                         assert np.array_equal(got.view(np.uint32), base.view(np.uint32)), (lp, vpt, block, bps, pdl)
+    finally:
+        gpu_ctx.set_tune(**saved)
+
+
+def test_resident_prefix_path_on_a_book_larger_than_l2(gpu_ctx):
+    """Load path 7 keeps a prefix of the book (about half the L2) resident
+    and streams the rest: on a 4M-option book (112 MB) both parts, and the
+    boundary between them, give the bits of the plain path."""
+    book = books.generate(4_000_001, seed=16)
+    saved = gpu_ctx.get_tune()
+    try:
+        gpu_ctx.set_tune(1, 256, 0, 0, 0)
+        base = gpu_ctx.price_book(book, num_runs=1)
+        for vpt, block, bps, pdl in ((1, 256, 0, 1), (2, 512, 4, 1), (1, 128, 8, 0)):
+            gpu_ctx.set_tune(vpt, block, bps, 7, pdl)
+            got = gpu_ctx.price_book(book, num_runs=3)
+            assert np.array_equal(got.view(np.uint32), base.view(np.uint32)), (vpt, block, bps, pdl)
     finally:
         gpu_ctx.set_tune(**saved)
 
