@@ -201,7 +201,10 @@ __device__ __forceinline__ float price_fast(float s, float k, float r, float v,
 // component is that of the scalar operation.  SFU approximations, compares
 // and selects stay per component.  The two components are therefore
 // bit-identical to price_fast on each option, with about half the issued
-// FP32 instructions.
+// FP32 instructions.  One caveat, measured: the toolchain fuses a packed
+// multiply into a packed add or subtract that is its only use, skipping the
+// product's rounding.  No product here has that shape: each is an fma
+// operand, is exact, or has several uses.
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
