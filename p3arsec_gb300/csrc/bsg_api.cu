@@ -271,7 +271,8 @@ int enqueue_map_runs(bsg_ctx* c, const bsg::SoA& a, int64_t n, int runs, int mod
     const bsg::MapCfg cfg = c->tune;
     if (runs == 1 || (flags & BSG_NO_GRAPH)) {
         for (int j = 0; j < runs; ++j) {
-            cudaError_t e = bsg::launch_map(a, n, mode, cfg, c->sm_count, c->stream);
+            cudaError_t e = bsg::launch_map(a, n, mode, bsg::pass_cfg(cfg, j, runs), c->sm_count,
+                                            c->stream);
             if (e != cudaSuccess) return cuda_fail(c, e, "launch_map");
             c->launches++;
         }
@@ -284,7 +285,7 @@ int enqueue_map_runs(bsg_ctx* c, const bsg::SoA& a, int64_t n, int runs, int mod
         BSG_CK(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         cudaError_t le = cudaSuccess;
         for (int j = 0; j < runs && le == cudaSuccess; ++j)
-            le = bsg::launch_map(a, n, mode, cfg, c->sm_count, c->stream);
+            le = bsg::launch_map(a, n, mode, bsg::pass_cfg(cfg, j, runs), c->sm_count, c->stream);
         cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
         if (le != cudaSuccess) {
             if (g) cudaGraphDestroy(g);
@@ -960,7 +961,9 @@ int bsg_price_books_plain(bsg_ctx* c, const float* s, const float* k, const floa
             if (!segs[i].len) continue;
             const uint64_t o = segs[i].offset;
             bsg::SoA b{s + o, k + o, r + o, v + o, t + o, otype + o, prices + o};
-            cudaError_t e = bsg::launch_map(b, (int64_t)segs[i].len, mode, c->tune, c->sm_count, c->stream);
+            cudaError_t e = bsg::launch_map(b, (int64_t)segs[i].len, mode,
+                                            bsg::pass_cfg(c->tune, j, num_runs), c->sm_count,
+                                            c->stream);
             if (e != cudaSuccess) return cuda_fail(c, e, "launch_map (per book)");
             c->launches++;
         }
@@ -1162,7 +1165,8 @@ extern "C" int bsg_autotune(bsg_ctx* c, size_t n, bsg_tune* out) {
         if (e != cudaSuccess) return -1.0f;
         cudaEventRecord(e0, c->stream);
         for (int i = 0; i < reps && e == cudaSuccess; ++i)
-            e = bsg::launch_map(a, (int64_t)n, bsg::MODE_FAST, cfg, c->sm_count, c->stream);
+            e = bsg::launch_map(a, (int64_t)n, bsg::MODE_FAST, bsg::pass_cfg(cfg, i, reps),
+                                c->sm_count, c->stream);
         cudaEventRecord(e1, c->stream);
         c->launches += reps + 1;
         if (e != cudaSuccess) return -1.0f;

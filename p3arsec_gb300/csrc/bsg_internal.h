@@ -61,6 +61,16 @@ constexpr int kBatchBlock = 256;
 // scalar kernel.  Returns the launch error.
 cudaError_t launch_map(const SoA& a, int64_t n, int mode, const MapCfg& cfg,
                        int sm_count, cudaStream_t st);
+// The shape of pass j of `runs` consecutive passes over the same book.  The
+// resident-prefix load path (7) marks part of the book evict_last so that it
+// stays in L2 for the next pass.  The last pass runs the same loads with
+// evict_first (6): it still hits the resident lines, and an access with an
+// explicit policy sets the line's priority, so no evict_last line is left
+// behind the call.  A single pass therefore never marks lines evict_last.
+inline MapCfg pass_cfg(MapCfg c, int j, int runs) {
+    if (c.load_path == 7 && j == runs - 1) c.load_path = 6;
+    return c;
+}
 // Reads and clears the bulk-staged kernel's error word (non-zero: a bounded
 // wait expired and some tiles were not priced).
 unsigned bulk_error_take();
