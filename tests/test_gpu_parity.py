@@ -136,15 +136,20 @@ def _dev(torch, book, pad=0):
     return arrs
 
 
-def test_device_pointers_and_misaligned_scalar_path(gpu_ctx):
+@pytest.mark.parametrize("mode", ["fast", "sfu_ref", "libm_ref"])
+def test_device_pointers_and_misaligned_scalar_path(gpu_ctx, mode):
+    """Pointers offset by 1 or 3 floats take the scalar kernel (one option
+    per thread, scalar arithmetic); aligned ones the vector kernel (packed
+    f32x2 arithmetic in the fast and libm modes): every mode gives the same
+    bits either way -- a packed product fused into a packed add would not."""
     torch = pytest.importorskip("torch")
-    book = books.generate(50001, seed=13)
-    host = gpu_ctx.price_book(book)
+    book = books.generate(50001, seed=13, dist="tails")
+    host = gpu_ctx.price_book(book, mode=mode)
     for pad in (0, 1, 3):
         d = _dev(torch, book, pad)
         out = torch.zeros(len(book) + pad, dtype=torch.float32, device="cuda:0")
         views = [x[pad:] for x in d]
-        gpu_ctx.price_soa(*views, out[pad:], n=len(book), num_runs=2, device=True)
+        gpu_ctx.price_soa(*views, out[pad:], n=len(book), num_runs=2, mode=mode, device=True)
         torch.cuda.synchronize()
         got = out[pad:].cpu().numpy()
         assert np.array_equal(got.view(np.uint32), host.view(np.uint32)), pad
