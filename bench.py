@@ -294,6 +294,13 @@ def run_ours(args, rank, world, local):
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
+    traffic = line["roofline"]["traffic"]
+    if traffic:
+        # the DRAM bytes ncu measured per pass over the event-timed pass: how
+        # close the pass runs to the copy bandwidth in the bytes it really
+        # moves (achieved counts the algorithmic 28 B/option)
+        line["roofline"]["traffic_gbs"] = traffic / per_launch_s / 1e9
+        line["roofline"]["traffic_frac"] = traffic / per_launch_s / 1e9 / peak
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(book)
     if rank == 0:
