@@ -367,7 +367,8 @@ __device__ __forceinline__ float cndf_libm_ref(float x) {
     const float np = dmul_finite(e, isp);                        // :157
     float k = dmul(x, c0);                                       // :159
     k = __fadd_rn(1.0f, k);                                      // :160
-    k = __fdiv_rn(1.0f, k);                                      // :161
+    k = __frcp_rn(k);  // :161, 1.0 / k in double rounded to float: the
+                       // correctly rounded reciprocal
     const float k2 = __fmul_rn(k, k), k3 = __fmul_rn(k2, k);     // :162-165
     const float k4 = __fmul_rn(k3, k), k5 = __fmul_rn(k4, k);
     float l1 = dmul_finite(k, c1);                               // :167
@@ -506,7 +507,7 @@ __device__ __forceinline__ float2 cndf_libm_ref2(float2 xin) {
     const float2 np = dmul_finite2(e, isp);
     float2 k = make_float2(dmul(x.x, c0), dmul(x.y, c0));
     k = add2(f2(1.0f), k);
-    k = make_float2(__fdiv_rn(1.0f, k.x), __fdiv_rn(1.0f, k.y));
+    k = make_float2(__frcp_rn(k.x), __frcp_rn(k.y));
     const float2 k2 = mul2(k, k), k3 = mul2(k2, k);
     const float2 k4 = mul2(k3, k), k5 = mul2(k4, k);
     float2 l1 = dmul_finite2(k, c1);
