@@ -3,6 +3,7 @@
 // expl/logl rounded to float.
 //
 //   crmath_check exp|log <stride> <threads>
+//   crmath_check special
 //
 // Walks every <stride>-th float of the function's domain (exp: [-87, 88.5];
 // log: positive normal floats) and prints one line:
@@ -60,7 +61,44 @@ void check_one(float x, long double exact, float got, Result& r) {
 
 }  // namespace
 
+// Special and out-of-domain arguments go to the platform's expf/logf and
+// must come back with their IEEE results.
+int check_special() {
+    const float inf = INFINITY, nan = NAN;
+    int bad = 0;
+    auto same = [&](const char* what, float got, float want) {
+        const bool ok = (std::isnan(want) && std::isnan(got)) || bits(got) == bits(want);
+        if (!ok) {
+            std::printf("special %s: got %a want %a\n", what, got, want);
+            ++bad;
+        }
+    };
+    same("exp(nan)", bsg_cr::exp(nan), nan);
+    same("exp(-inf)", bsg_cr::exp(-inf), 0.0f);
+    same("exp(inf)", bsg_cr::exp(inf), inf);
+    same("exp(0)", bsg_cr::exp(0.0f), 1.0f);
+    same("exp(-0)", bsg_cr::exp(-0.0f), 1.0f);
+    same("exp(-100)", bsg_cr::exp(-100.0f), expf(-100.0f));
+    same("exp(-104)", bsg_cr::exp(-104.0f), expf(-104.0f));
+    same("exp(89)", bsg_cr::exp(89.0f), expf(89.0f));
+    same("exp(88.5)", bsg_cr::exp(88.5f), (float)expl(88.5L));
+    same("exp(-87)", bsg_cr::exp(-87.0f), (float)expl(-87.0L));
+    same("log(nan)", bsg_cr::log(nan), nan);
+    same("log(0)", bsg_cr::log(0.0f), -inf);
+    same("log(-0)", bsg_cr::log(-0.0f), -inf);
+    same("log(-1)", bsg_cr::log(-1.0f), nan);
+    same("log(inf)", bsg_cr::log(inf), inf);
+    same("log(1)", bsg_cr::log(1.0f), 0.0f);
+    same("log(denorm_min)", bsg_cr::log(from_bits(1)), logf(from_bits(1)));
+    same("log(subnormal)", bsg_cr::log(from_bits(0x00400000u)), logf(from_bits(0x00400000u)));
+    same("log(FLT_MIN)", bsg_cr::log(from_bits(0x00800000u)), (float)logl((long double)from_bits(0x00800000u)));
+    same("log(FLT_MAX)", bsg_cr::log(from_bits(0x7F7FFFFFu)), (float)logl((long double)from_bits(0x7F7FFFFFu)));
+    std::printf("special checked, %d bad\n", bad);
+    return bad ? 1 : 0;
+}
+
 int main(int argc, char** argv) {
+    if (argc == 2 && std::strcmp(argv[1], "special") == 0) return check_special();
     if (argc != 4) {
         std::printf("usage: crmath_check exp|log <stride> <threads>\n");
         return 2;

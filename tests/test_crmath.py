@@ -36,6 +36,14 @@ def test_correctly_rounded_on_a_strided_walk(checker, fn):
     assert mis <= checked * 1e-6 and max_ulp <= 1, r.stdout
 
 
+def test_special_arguments_take_the_platform_functions(checker):
+    """NaN, infinities, zeros, negative and subnormal arguments, and results
+    beyond the float range come back as IEEE expf/logf give them."""
+    r = subprocess.run([checker, "special"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
+                       text=True, timeout=60)
+    assert r.returncode == 0, r.stdout
+
+
 def test_table_header_is_what_the_generator_writes(tmp_path):
     """bsg_crmath_tables.h is generated: regenerating it changes nothing."""
     import importlib.util
