@@ -57,7 +57,7 @@ typedef enum bsg_status {
 #define BSG_MODE_LIBM_REF 0x020u /* reference operation order, correctly rounded exp/log,
                                     IEEE division and square root: the reference's own
                                     FP32 prices wherever glibc's expf/logf round correctly
-                                    (99.7 % of options); compute-bound, ~3.8x slower */
+                                    (99.7 % of options); compute-bound, ~3x slower */
 #define BSG_MODE_MASK     0x0F0u
 #define BSG_NO_GRAPH      0x100u /* launch NUM_RUNS kernels directly, no graph */
 

@@ -433,9 +433,11 @@ __device__ __forceinline__ bool cr_log_in_range(float x) {
     return x >= 1.17549435e-38f && x <= 3.40282347e38f;
 }
 
-__device__ __forceinline__ float2 cr_exp2(float2 x) {
-    if (!(cr_exp_in_range(x.x) && cr_exp_in_range(x.y)))
-        return make_float2(bsg_cr::exp(x.x), bsg_cr::exp(x.y));
+// A lane whose argument is outside bsg_cr::exp's domain takes the platform's
+// expf, as bsg_cr::exp does; the packed evaluation runs on 0 in its place.
+__device__ __forceinline__ float2 cr_exp2(float2 xin) {
+    const bool in0 = cr_exp_in_range(xin.x), in1 = cr_exp_in_range(xin.y);
+    const float2 x = make_float2(in0 ? xin.x : 0.0f, in1 ? xin.y : 0.0f);
     const float2 sh = fma2(x, f2(BSG_CR_INV_L), f2(bsg_cr::kShifter));
     const float2 nf = sub2(sh, f2(bsg_cr::kShifter));
     const int n0 = (int)(__float_as_uint(sh.x) - bsg_cr::kShifterBits);
@@ -458,8 +460,11 @@ __device__ __forceinline__ float2 cr_exp2(float2 x) {
     const FF2 sm = fast_two_sum2(thi, tq.hi);
     const float2 lo = add2(sm.lo, add2(tq.lo, add2(tlo, fma2(thi, ql, mul2(tlo, q.hi)))));
     const float2 y = add2(sm.hi, lo);
-    return mul2(y, make_float2(__uint_as_float((uint32_t)((n0 >> 5) + 127) << 23),
-                               __uint_as_float((uint32_t)((n1 >> 5) + 127) << 23)));
+    float2 e = mul2(y, make_float2(__uint_as_float((uint32_t)((n0 >> 5) + 127) << 23),
+                                   __uint_as_float((uint32_t)((n1 >> 5) + 127) << 23)));
+    if (!in0) e.x = bsg_cr::fallback_exp(xin.x);
+    if (!in1) e.y = bsg_cr::fallback_exp(xin.y);
+    return e;
 }
 
 __device__ __forceinline__ float2 cr_log2(float2 x) {
