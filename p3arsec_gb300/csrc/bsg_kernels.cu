@@ -7,7 +7,10 @@
 //  * SoA streams read with 128-bit (v4) or 256-bit (v8) non-coherent loads
 //    that do not allocate in L1, optionally inserted into L2 as evict_first
 //    (a cyclic scan of a working set larger than L2 then keeps a slice of it
-//    resident between passes); prices stored with streaming stores.
+//    resident between passes), or with a prefix of the book (about half the
+//    L2, inputs and prices) evict_last and the rest evict_first, so that
+//    the prefix stays resident from pass to pass; prices stored with
+//    streaming stores (or with the prefix's policy).
 //  * Each thread loads VPT vector groups of all six arrays before computing,
 //    so a warp keeps 6 * VPT independent 512/1024-byte requests in flight.
 //  * Grid: one block per tile, or a persistent grid-stride loop sized in
