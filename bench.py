@@ -5,13 +5,24 @@ Default workload (the headline): the plain map over 10,000,000 seeded options
 (S~U[10,200], K=S*U[0.5,1.5], r~U[0.01,0.10], v~U[0.05,0.65], t~U[0.05,2],
 calls/puts 50/50), FP32, NUM_RUNS = 100 passes per step -- one step is one
 whole ROI of the reference benchmark (blackscholes.c:781-913).  The 280 MB
-working set is larger than the 129 MB L2, so every pass streams from HBM.
+working set is larger than the 129 MB L2, but only 2.2x: cross-pass L2 hits
+serve part of it (the line says so), so the same line carries three nested
+records measured in the same run:
+
+* ``roofline_2p28`` -- the map over 2^28 options (7.5 GB, 58x the L2): the
+  HBM-roofline fraction with nothing L2-resident;
+* ``batch`` -- 4,096 books of log-uniform size in one persistent CUDA-graph
+  launch per pass vs one plain launch per book per pass;
+* ``serve`` -- an open-loop Poisson trace through the continuous-batching
+  server vs one plain launch per request, with the throughput each sustains
+  under p99 bounds of 0.5, 1 and 2 ms (medians of repeated traces).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--config map|batch|precision|serve]
+                    [--config map|batch|precision|serve|io|fp64|prefix-sweep]
 
 One JSON line on stdout (rank 0).  Under torchrun each rank prices its own
-book on its own GPU (weak scaling, no collective on the data path).
+book on its own GPU (weak scaling, no collective on the data path); the
+nested records are measured at one GPU only.
 """
 from __future__ import annotations
 
@@ -29,20 +40,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_OPTIONS = 10_000_000
+N_2P28 = 1 << 28
 NUM_RUNS = 100
 BYTES_PER_OPTION = 28  # 5 float inputs + int32 otype + float price
 METRIC = "options/sec & %HBM roofline"
 UNIT = "options/s"
 SEED = 20241203
-# Steady-state DRAM bytes per pass of the fast map kernel by (load path,
-# options), from warm ncu captures (dram__bytes_read.sum +
-# dram__bytes_write.sum of mid-run launches) summarised in
-# profiles/map_fast_10M.md.  The L2 keeps a fixed slice of the working set
-# between passes, so traffic is not proportional to the options: sizes and
-# shapes not captured report null.
-NCU_DRAM_BYTES_PER_PASS = {(1, 10_000_000): 206.0e6, (2, 10_000_000): 266.1e6,
-                           (6, 10_000_000): 206.9e6, (7, 10_000_000): 228.9e6}
-NCU_PROFILE = "profiles/map_fast_10M.md"
+L2_FALLBACK = 126.5e6  # bytes, when the device does not report its L2
 
 
 # ------------------------------------------------------------------ ranks
@@ -165,6 +169,12 @@ def measured_hbm_peak():
 
 
 # -------------------------------------------------------------- CPU baseline
+PORT_NOTE = ("the oracle port of the reference's FastFlow map (blackscholes.c:315-348): the "
+             "reference's FP32 arithmetic bit for bit, FastFlow's static partition, a join per "
+             "pass, on this host's cores; the reference's own build needs its source tree, which "
+             "is not on this host")
+
+
 def cpu_baseline(book, target_s: float = 10.0):
     """The oracle port of the reference's FastFlow map on every host core,
     over the same book, with as many passes as fit in ~target_s seconds."""
@@ -175,7 +185,59 @@ def cpu_baseline(book, target_s: float = 10.0):
     _, secs = oracle.bs_map(book, threads, runs)
     return {"value": len(book) * runs / secs, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{len(book)} options x {runs} passes (of {NUM_RUNS}) of the same book, "
-                      f"static partition over {threads} threads, {secs:.2f} s"}
+                      f"static partition over {threads} threads, {secs:.2f} s",
+            "note": PORT_NOTE}
+
+
+def map_config(n: int, runs: int, world: int) -> dict:
+    """The workload description both arms print for the map."""
+    ws = BYTES_PER_OPTION * n
+    return {"workload": f"plain map, {n} European options FP32 SoA, NUM_RUNS={runs} "
+                        "passes per step", "options": n, "num_runs": runs,
+            "parallelism": f"replicas x{world} (independent books)",
+            "l2": (f"inputs ({ws / 1e6:.0f} MB) larger than L2 (129 MB); no flush"
+                   if ws > 129e6 else
+                   f"inputs ({ws / 1e6:.1f} MB) fit in L2 (129 MB): an L2-resident run, "
+                   "not an HBM measurement"),
+            "mode": "fast"}
+
+
+def l2_bytes(device: int) -> float:
+    import torch
+    v = getattr(torch.cuda.get_device_properties(device), "L2_cache_size", 0)
+    return float(v) if v else L2_FALLBACK
+
+
+def prefix_bytes(tune: dict, n: int, l2: float) -> int:
+    """Bytes of the book the resident-prefix load path keeps in L2 (the
+    library's rule: resident_32nds of the L2, whole 8-option groups)."""
+    if tune.get("load_path") != 7:
+        return 0
+    r32 = tune.get("resident_32nds") or 15
+    groups = int(l2) * r32 // 32 // (BYTES_PER_OPTION * 8)
+    return min(groups, n // 8) * 8 * BYTES_PER_OPTION
+
+
+def time_steps(stream, step, steps, warmup, clocks_device=None):
+    """warmup untimed steps, then `steps` timed with CUDA events on `stream`;
+    returns (seconds, clock summary or None)."""
+    import torch
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    clk = ClockSampler(clocks_device) if clocks_device is not None else None
+    if clk:
+        clk.__enter__()
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    e1.synchronize()
+    if clk:
+        clk.__exit__(None, None, None)
+    return e0.elapsed_time(e1) / 1e3, (clk.summary() if clk else None)
 
 
 # ------------------------------------------------------------------ our arm
@@ -227,6 +289,7 @@ def run_ours(args, rank, world, local):
     per_launch_s = secs / (runs * args.steps)
     achieved = BYTES_PER_OPTION * n / per_launch_s / 1e9
     peak, peak_src = measured_hbm_peak()
+    l2 = l2_bytes(local)
 
     # accuracy of the timed output against the FP64 oracle kernel
     accuracy = None
@@ -268,46 +331,104 @@ def run_ours(args, rank, world, local):
                "synchronous": {"value": world * n * runs * args.steps / sync_s,
                                "ms_per_step": 1e3 * sync_s / args.steps}}
 
+    ws = BYTES_PER_OPTION * n
+    pb = prefix_bytes(tune, n, l2)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded book, reference config distributions)",
-        "config": {"workload": f"plain map, {n} European options FP32 SoA, NUM_RUNS={runs} "
-                               "passes per step", "options": n, "num_runs": runs,
-                   "parallelism": f"replicas x{world} (independent books)",
-                   "l2": (f"inputs ({BYTES_PER_OPTION * n / 1e6:.0f} MB) larger than L2 "
-                          "(129 MB); no flush" if BYTES_PER_OPTION * n > 129e6 else
-                          f"inputs ({BYTES_PER_OPTION * n / 1e6:.1f} MB) fit in L2 (129 MB): "
-                          "an L2-resident run, not an HBM measurement"),
-                   "tune": tune, "mode": "fast"},
+        "config": map_config(n, runs, world),
+        "tune": tune,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src,
-                     "traffic": NCU_DRAM_BYTES_PER_PASS.get((tune["load_path"], n)),
-                     "traffic_source": (NCU_PROFILE + " (warm, steady state)"
-                                        if (tune["load_path"], n) in NCU_DRAM_BYTES_PER_PASS
-                                        else None),
-                     "bytes_per_launch": BYTES_PER_OPTION * n,
-                     "avg_launch_us": per_launch_s * 1e6},
+                     "traffic": None,
+                     "traffic_note": "DRAM bytes per pass are measured with ncu (serialised "
+                                     "launches), not in this run; they are summarised with "
+                                     "the kernel's profile",
+                     "bytes_per_launch": ws, "avg_launch_us": per_launch_s * 1e6,
+                     "l2_assisted": bool(ws < 4 * l2),
+                     "l2_bytes": int(l2), "prefix_bytes": pb,
+                     "note": ("achieved counts the algorithmic 28 B/option; the book is "
+                              f"{ws / l2:.1f}x the L2, so lines kept in L2 from pass to pass "
+                              "(the resident prefix and the evict-first slice) serve part of "
+                              "each pass and frac can exceed 1; roofline_2p28 is the fraction "
+                              "with nothing L2-resident")
+                     if ws < 4 * l2 else "the book is far larger than the L2"},
         "accuracy": accuracy,
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
-    traffic = line["roofline"]["traffic"]
-    if traffic:
-        # the DRAM bytes ncu measured per pass over the event-timed pass: how
-        # close the pass runs to the copy bandwidth in the bytes it really
-        # moves (achieved counts the algorithmic 28 B/option)
-        line["roofline"]["traffic_gbs"] = traffic / per_launch_s / 1e9
-        line["roofline"]["traffic_frac"] = traffic / per_launch_s / 1e9 / peak
+    ctx.close()
+    del dev, out
+    torch.cuda.empty_cache()
+    if world == 1 and not args.no_nested:
+        line["roofline_2p28"] = _nested(map_2p28_record, args, local, peak, peak_src)
+        line["batch"] = _nested(batch_record, args, local, steps=3, warmup=3)
+        line["serve"] = _nested(serve_record, args, local)
+        torch.cuda.empty_cache()
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(book)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def _nested(fn, *a, **kw):
+    """A nested record, or the error that stopped it (the headline stands)."""
+    try:
+        return fn(*a, **kw)
+    except Exception as ex:  # noqa: BLE001 -- reported in the JSON line
+        import traceback
+        traceback.print_exc(file=sys.stderr)
+        return {"error": f"{type(ex).__name__}: {ex}"}
+
+
+def map_2p28_record(args, local, peak, peak_src, n=N_2P28, steps=3, warmup=3):
+    """The fast map over 2^28 options (7.5 GB: nothing of the book can stay
+    in L2 between passes), NUM_RUNS passes per step, autotuned at that
+    size: the HBM-roofline fraction of the map."""
+    import torch
+
+    from p3arsec_gb300 import Context, books
+    ctx = Context(local, max_options=1)
+    tune = ctx.autotune(n)
+    dev = books.generate_device(n, SEED + 28, device=f"cuda:{local}")
+    out = torch.empty(n, dtype=torch.float32, device=f"cuda:{local}")
+    stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{local}")
+    runs = args.runs
+
+    def step():
+        ctx.price_soa(*dev, out, n=n, num_runs=runs, device=True, asynchronous=True)
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    l0 = ctx.launches
+    secs, clk = time_steps(stream, step, steps, 0, clocks_device=local)
+    launches = ctx.launches - l0
+    per_launch_s = secs / (runs * steps)
+    achieved = BYTES_PER_OPTION * n / per_launch_s / 1e9
+    edges = np.array([0.0, 0.5, 1.0, 2.0, 3.0, 4.0, 6.0, np.inf])
+    rep = ctx.error_report(dev, out, n, edges)
+    l2 = l2_bytes(local)
+    rec = {"workload": f"plain map, {n} options FP32 SoA ({BYTES_PER_OPTION * n / 1e9:.2f} GB, "
+                       f"{BYTES_PER_OPTION * n / l2:.0f}x the L2), NUM_RUNS={runs} passes per step, "
+                       "plain distribution drawn on the GPU",
+           "options": n, "num_runs": runs, "steps": steps, "warmup": warmup,
+           "value": n * runs * steps / secs, "unit": UNIT, "ms_per_step": 1e3 * secs / steps,
+           "tune": tune, "prefix_bytes": prefix_bytes(tune, n, l2),
+           "bound": "hbm", "achieved": achieved, "peak": peak, "peak_source": peak_src,
+           "unit_bw": "GB/s", "frac": achieved / peak, "avg_launch_us": per_launch_s * 1e6,
+           "bytes_per_launch": BYTES_PER_OPTION * n, "gpu_launches": launches,
+           "max_abs_vs_fp64": max(x["max_abs"] for x in rep),
+           "clocks": clk}
+    ctx.close()
+    del dev, out
+    torch.cuda.empty_cache()
+    return rec
 
 
 # ------------------------------------------------------------ batched books
@@ -317,25 +438,24 @@ def book_sizes(nbooks: int, seed: int, lo: int = 1, hi: int = 1 << 20):
     return np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi + 1), nbooks))).astype(np.int64).clip(lo, hi)
 
 
-def run_batch(args, rank, world, local):
+def batch_record(args, local, steps=None, warmup=None, nbooks=None, seed=SEED + 4):
     """Config 4: many uneven books in one pool, one persistent CUDA-graph
-    launch per pass vs one plain launch per book per pass."""
+    launch per pass vs one plain launch per book per pass (both NUM_RUNS
+    passes per step, the same device pool, outputs compared bit for bit)."""
     import torch
 
     from p3arsec_gb300 import Context, books
-    from p3arsec_gb300 import build as b
-    b.build()
-    torch.cuda.set_device(local)
-    sizes = book_sizes(args.books, SEED + 4)
+    steps = args.steps if steps is None else steps
+    warmup = args.warmup if warmup is None else warmup
+    nbooks = args.books if nbooks is None else nbooks
+    sizes = book_sizes(nbooks, seed)
     segs, off = [], 0
     for nb in sizes:
         segs.append((off, int(nb)))
         off += (int(nb) + 63) // 64 * 64  # books start 256-byte aligned
     pool_len = off
     total = int(sizes.sum())
-    book = books.generate(pool_len, seed=SEED + 5)
-    dev = [torch.from_numpy(a).to(f"cuda:{local}") for a in book.arrays()]
-    del book
+    dev = books.generate_device(pool_len, seed + 1, device=f"cuda:{local}")
     out_b = torch.zeros(pool_len, dtype=torch.float32, device=f"cuda:{local}")
     out_p = torch.zeros(pool_len, dtype=torch.float32, device=f"cuda:{local}")
     ctx = Context(local, max_options=1)
@@ -353,50 +473,64 @@ def run_batch(args, rank, world, local):
         batch_tune = ctx.autotune_batch(dev, out_b, pool_len, segs)
 
     def timed(fn):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             fn()
         torch.cuda.synchronize()
         l0 = ctx.launches
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        with ClockSampler(local) as clk:
-            e0.record(stream)
-            for _ in range(args.steps):
-                fn()
-            e1.record(stream)
-            e1.synchronize()
-        return e0.elapsed_time(e1) / 1e3, ctx.launches - l0, clk.summary()
+        secs, clk = time_steps(stream, fn, steps, 0, clocks_device=local)
+        return secs, ctx.launches - l0, clk
 
-    secs_b, launches_b, clk = timed(lambda: ctx.price_batch(dev, out_b, pool_len, segs, num_runs=runs,
-                                                            asynchronous=True))
-    secs_p, launches_p, _ = timed(lambda: ctx.price_batch(dev, out_p, pool_len, segs, num_runs=runs,
-                                                          plain=True, asynchronous=True))
+    secs_b, launches_b, clk = timed(lambda: ctx.price_batch(dev, out_b, pool_len, segs,
+                                                            num_runs=runs, asynchronous=True))
+    secs_p, launches_p, _ = timed(lambda: ctx.price_batch(dev, out_p, pool_len, segs,
+                                                          num_runs=runs, plain=True,
+                                                          asynchronous=True))
     torch.cuda.synchronize()
     same = bool(torch.equal(out_b.view(torch.int32), out_p.view(torch.int32)))
-    value = total * runs * args.steps / secs_b
-    plain = total * runs * args.steps / secs_p
+    value = total * runs * steps / secs_b
+    plain = total * runs * steps / secs_p
     peak, peak_src = measured_hbm_peak()
-    achieved = BYTES_PER_OPTION * total * runs * args.steps / secs_b / 1e9
-    line = {
-        "metric": "options/sec (batched books, one persistent launch per pass)", "value": value,
-        "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * secs_b / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded books)",
-        "config": {"workload": f"{args.books} books, sizes log-uniform in [1, 2^20], "
-                               f"{total} options, {runs} passes per step",
-                   "books": args.books, "options": total, "num_runs": runs,
-                   "tune_plain": ctx.get_tune(), "tune_batch": batch_tune},
-        "plain_per_book": {"value": plain, "unit": UNIT, "ms_per_step": 1e3 * secs_p / args.steps,
+    achieved = BYTES_PER_OPTION * total * runs * steps / secs_b / 1e9
+    rec = {
+        "workload": f"{nbooks} books, sizes log-uniform in [1, 2^20] (seed {seed}), "
+                    f"{total} options, {runs} passes per step",
+        "books": nbooks, "options": total, "num_runs": runs, "seed": seed,
+        "steps": steps, "warmup": warmup,
+        "value": value, "unit": UNIT, "ms_per_step": 1e3 * secs_b / steps,
+        "plain_per_book": {"value": plain, "unit": UNIT, "ms_per_step": 1e3 * secs_p / steps,
                            "gpu_launches": launches_p},
         "speedup_vs_plain": value / plain,
-        "bitwise_equal_to_plain": same,
+        "bit_identical": same,
+        "tune_plain": ctx.get_tune(), "tune_batch": batch_tune,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src},
         "gpu_launches": launches_b, "clocks": clk,
     }
+    ctx.close()
+    del dev, out_b, out_p
+    torch.cuda.empty_cache()
+    return rec
+
+
+def run_batch(args, rank, world, local):
+    """--config batch: the batched-books record as its own JSON line."""
+    import torch
+
+    from p3arsec_gb300 import build as b
+    b.build()
+    torch.cuda.set_device(local)
+    rec = batch_record(args, local)
+    line = {"metric": "options/sec (batched books, one persistent launch per pass)",
+            "value": rec["value"], "unit": UNIT, "n_gpus": world, "steps": rec["steps"],
+            "warmup": rec["warmup"], "ms_per_step": rec["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded books)",
+            "config": {"workload": rec["workload"], "books": rec["books"],
+                       "options": rec["options"], "num_runs": rec["num_runs"]},
+            **{k: rec[k] for k in ("plain_per_book", "speedup_vs_plain", "bit_identical",
+                                   "tune_plain", "tune_batch", "roofline", "gpu_launches",
+                                   "clocks")}}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
 
 
 # --------------------------------------------------------- precision sweep
@@ -481,78 +615,134 @@ def host_link_bandwidth(device: int):
     del h, d
     return res
 
-def run_serve(args, rank, world, local):
-    """Config 5: open-loop Poisson trace, request sizes log-uniform in
-    [16, 2^20], 64 GB device admission budget; the continuous-batching loop
-    vs one plain launch per request, over a sweep of arrival rates."""
+SERVE_BOUNDS_MS = (0.5, 1.0, 2.0)
+
+
+def serve_host_pool(local, pool_n=1 << 24):
+    """A pinned host pool of pool_n options (drawn on the GPU, copied out)
+    that the traces slice their requests from, and a pinned prices array."""
     import torch
 
-    from p3arsec_gb300 import abi, books
+    from p3arsec_gb300 import books
+    dev = books.generate_device(pool_n, SEED + 6, device=f"cuda:{local}")
+    host = [x.cpu().pin_memory().numpy() for x in dev]
+    del dev
+    out = torch.zeros(pool_n, dtype=torch.float32).pin_memory().numpy()
+    return host, out
+
+
+def serve_point(host, out, mode, rate, seconds, args, local, seed):
+    from p3arsec_gb300 import abi
+    lo_n, hi_n = (int(x) for x in args.serve_sizes.split(","))
+    return abi.serve_trace(host, out, rate_per_s=rate, duration_s=seconds, min_n=lo_n,
+                           max_n=hi_n, seed=seed, device=local, budget_bytes=64 << 30,
+                           max_inflight=args.serve_inflight, plain=(mode == "plain"),
+                           drain_timeout_s=60.0,
+                           fused=(mode == "batched" and args.serve_fused >= 1),
+                           persistent=(mode == "batched" and args.serve_fused == 2))
+
+
+def serve_record(args, local, repeats=3, trace_rate=20000.0, trace_seconds=5.0,
+                 batched_rates=(50000, 55000, 60000, 65000, 70000, 75000, 80000),
+                 plain_rates=(1000, 2500, 5000, 7500, 10000, 12500, 15000)):
+    """Config 5 in bounded form: (1) the specified trace (Poisson arrivals at
+    20k requests/s, sizes log-uniform in [16, 2^20], 64 GB budget) for
+    trace_seconds through the continuous-batching server and through the
+    plain loop (one request at a time: copies, one launch, copy back);
+    (2) the throughput each loop sustains with p99 under 0.5, 1 and 2 ms:
+    traces at several rates, each repeated `repeats` times, the median p99
+    and median throughput per rate; a loop's figure for a bound is its best
+    median throughput whose median p99 stays under the bound.  The host
+    link caps the batched loop (24 B/option inbound), so the ratio at a bound
+    can be no larger than link options/s over the plain loop's figure."""
+    host, out = serve_host_pool(local)
+    trace = {}
+    for mode in ("batched", "plain"):
+        r = serve_point(host, out, mode, trace_rate, trace_seconds, args, local, SEED + 20)
+        trace[mode] = {"requests": r["requests"], "completed": r["completed"],
+                       "options_per_s": r["options_per_s"], "p50_ms": 1e3 * r["p50_s"],
+                       "p99_ms": 1e3 * r["p99_s"], "p999_ms": 1e3 * r["p999_s"],
+                       "max_ms": 1e3 * r["max_s"],
+                       "late_submit_max_ms": 1e3 * r["late_submit_max_s"]}
+    sweep = {}
+    for mode, rates in (("batched", batched_rates), ("plain", plain_rates)):
+        pts = []
+        for rate in rates:
+            secs = float(min(3.0, max(1.0, 4000.0 / rate)))
+            reps = [serve_point(host, out, mode, rate, secs, args, local, SEED + int(rate) + 7 * k)
+                    for k in range(repeats)]
+            ok = all(x["completed"] == x["requests"] for x in reps)
+            pts.append({"rate_per_s": rate, "seconds": secs,
+                        "requests": [x["requests"] for x in reps],
+                        "p99_ms": [round(1e3 * x["p99_s"], 4) for x in reps],
+                        "p50_ms": [round(1e3 * x["p50_s"], 4) for x in reps],
+                        "median_p99_ms": float(np.median([1e3 * x["p99_s"] for x in reps])),
+                        "median_options_per_s": float(np.median([x["options_per_s"] for x in reps])),
+                        "late_submit_max_ms": round(1e3 * max(x["late_submit_max_s"] for x in reps), 3),
+                        "all_completed": ok})
+        sweep[mode] = pts
+
+    def best(mode, bound_ms):
+        ok = [p for p in sweep[mode] if p["all_completed"] and p["median_p99_ms"] <= bound_ms]
+        return max(ok, key=lambda p: p["median_options_per_s"]) if ok else None
+
+    link = host_link_bandwidth(local)
+    link_opts = link["h2d_GBps"] * 1e9 / 24
+    equal = []
+    for bound in SERVE_BOUNDS_MS:
+        bb, pp = best("batched", bound), best("plain", bound)
+        equal.append({
+            "p99_bound_ms": bound,
+            "batched_options_per_s": bb["median_options_per_s"] if bb else None,
+            "batched_rate_per_s": bb["rate_per_s"] if bb else None,
+            "plain_options_per_s": pp["median_options_per_s"] if pp else None,
+            "plain_rate_per_s": pp["rate_per_s"] if pp else None,
+            "ratio": (bb["median_options_per_s"] / pp["median_options_per_s"]) if (bb and pp) else None,
+            "ratio_ceiling_from_link": (link_opts / pp["median_options_per_s"]) if pp else None})
+    sat = max(p["median_options_per_s"] for p in sweep["batched"])
+    return {
+        "workload": f"open-loop Poisson trace at {trace_rate:g} req/s for {trace_seconds:g} s, "
+                    f"sizes log-uniform in [{args.serve_sizes.replace(',', ', ')}], 64 GB device "
+                    "budget; equal-p99 sweep: medians of "
+                    f"{repeats} traces per rate",
+        "batched_path": {0: "gather, batch kernel, scatter", 1: "one fused kernel per batch",
+                         2: "persistent kernel over a host-memory request ring"}[args.serve_fused],
+        "plain_path": "one thread, one request at a time: six H2D copies, one plain map launch, "
+                      "one D2H copy, event polled",
+        "trace": trace,
+        "throughput_at_equal_p99": equal,
+        "host_link": link,
+        "roofline": {"bound": "host link (H2D)", "achieved": sat * 24 / 1e9,
+                     "peak": link["h2d_GBps"], "unit": "GB/s",
+                     "frac": sat * 24 / 1e9 / link["h2d_GBps"],
+                     "note": "peak measured live: pinned host-to-device copy of 1 GiB; "
+                             "achieved = the best median batched options/s of the sweep x 24 B "
+                             "inbound per option"},
+        "sweep": sweep,
+    }
+
+
+def run_serve(args, rank, world, local):
+    """--config serve: the serving record as its own JSON line, with the
+    sweep of arrival rates given on the command line."""
+    import torch
+
     from p3arsec_gb300 import build as b
     b.build()
     torch.cuda.set_device(local)
-    pool_n = 1 << 24
-    book = books.generate(pool_n, seed=SEED + 6)
-    host = [torch.from_numpy(a).pin_memory().numpy() for a in book.arrays()]
-    out = torch.zeros(pool_n, dtype=torch.float32).pin_memory().numpy()
-    rates = [float(x) for x in args.serve_rates.split(",")]
-    lo_n, hi_n = (int(x) for x in args.serve_sizes.split(","))
-    sweep = {"batched": [], "plain": []}
-    for mode in ("batched", "plain"):
-        for rate in rates:
-            res = abi.serve_trace(host, out, rate_per_s=rate, duration_s=args.serve_seconds,
-                                  min_n=lo_n, max_n=hi_n, seed=SEED + int(rate),
-                                  device=local, budget_bytes=64 << 30,
-                                  max_inflight=args.serve_inflight,
-                                  plain=(mode == "plain"), drain_timeout_s=60.0,
-                                  fused=(mode == "batched" and args.serve_fused >= 1),
-                                  persistent=(mode == "batched" and args.serve_fused == 2))
-            res["rate_per_s"] = rate
-            sweep[mode].append(res)
-            print(json.dumps({"serve_point": mode, **res}), file=sys.stderr, flush=True)
-    at = {m: next((r for r in sweep[m] if r["rate_per_s"] == args.serve_rate), sweep[m][-1])
-          for m in sweep}
-
-    def best_at(mode, p99_cap):
-        ok = [r for r in sweep[mode] if r["completed"] == r["requests"] and r["p99_s"] <= p99_cap]
-        return max(ok, key=lambda r: r["options_per_s"]) if ok else None
-
-    # throughput at equal p99: for each latency bound, the best sustained
-    # throughput of each loop whose p99 stays under it
-    equal = []
-    for cap_ms in (0.25, 0.5, 1.0, 2.0, 5.0, 10.0):
-        bb, pp = best_at("batched", cap_ms / 1e3), best_at("plain", cap_ms / 1e3)
-        equal.append({"p99_bound_ms": cap_ms,
-                      "batched_options_per_s": bb["options_per_s"] if bb else None,
-                      "plain_options_per_s": pp["options_per_s"] if pp else None,
-                      "ratio": (bb["options_per_s"] / pp["options_per_s"]) if (bb and pp) else None})
-    # the serving roofline is the host link: inputs 24 B/option in, prices 4 B out
-    link = host_link_bandwidth(local)
-    sat = max(r["options_per_s"] for r in sweep["batched"])
-    a = at["batched"]
-    line = {
-        "metric": "serving: options/s with p50/p99/p99.9 latency vs plain per-request launch",
-        "value": a["options_per_s"], "unit": UNIT, "n_gpus": world,
-        "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded trace and books)",
-        "config": {"workload": f"open-loop Poisson trace at {args.serve_rate:g} req/s for "
-                               f"{args.serve_seconds:g} s, sizes log-uniform in [{lo_n}, {hi_n}], "
-                               f"64 GB device budget, {args.serve_inflight} batches in flight",
-                   "batched_path": {0: "gather, batch kernel, scatter",
-                                    1: "one fused kernel per batch",
-                                    2: "persistent kernel over a host-memory request ring"}
-                                   [args.serve_fused],
-                   "rates_swept": rates, "seconds_per_point": args.serve_seconds},
-        "latency_s": {"p50": a["p50_s"], "p99": a["p99_s"], "p999": a["p999_s"], "max": a["max_s"]},
-        "plain_at_rate": {k: at["plain"][k] for k in ("options_per_s", "p50_s", "p99_s", "p999_s",
-                                                      "completed", "requests")},
-        "throughput_at_equal_p99": equal,
-        "roofline": {"bound": "host link (H2D)", "achieved": sat * 24 / 1e9,
-                     "peak": link["h2d_GBps"], "unit": "GB/s", "frac": sat * 24 / 1e9 / link["h2d_GBps"],
-                     "note": "peak measured live: pinned host to device copy of 1 GiB; achieved = "
-                             "highest batched options/s in the sweep x 24 B inbound"},
-        "host_link": link,
-        "sweep": sweep,
-    }
+    brates = [float(x) for x in args.serve_batched_rates.split(",")]
+    prates = [float(x) for x in args.serve_plain_rates.split(",")]
+    rec = serve_record(args, local, repeats=args.serve_repeats, trace_rate=args.serve_rate,
+                       trace_seconds=args.serve_seconds, batched_rates=brates,
+                       plain_rates=prates)
+    t = rec["trace"]["batched"]
+    line = {"metric": "serving: options/s with p50/p99/p99.9 latency vs plain per-request launch",
+            "value": t["options_per_s"], "unit": UNIT, "n_gpus": world, "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic (seeded trace and books)",
+            "config": {"workload": rec["workload"], "batched_path": rec["batched_path"],
+                       "plain_path": rec["plain_path"]},
+            **{k: rec[k] for k in ("trace", "throughput_at_equal_p99", "host_link", "roofline",
+                                   "sweep")}}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -680,6 +870,59 @@ def run_io(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------- resident-prefix sweep
+def run_prefix_sweep(args, rank, world, local):
+    """The map over one book for every (shape, resident prefix size): the
+    resident-prefix load path (7) with resident_32nds 32nds of the L2, and
+    the same shape with every line evict-first (6) for 0.  Each point is
+    `steps` timed steps of NUM_RUNS passes after the warm-up steps.  The
+    autotuner searches the same sizes on its best resident-prefix shape."""
+    import torch
+
+    from p3arsec_gb300 import Context, books
+    from p3arsec_gb300 import build as b
+    b.build()
+    torch.cuda.set_device(local)
+    n, runs = args.n, args.runs
+    dev = (books.generate_device(n, SEED, device=f"cuda:{local}") if n > (1 << 24) else
+           [torch.from_numpy(a).to(f"cuda:{local}") for a in books.generate(n, seed=SEED).arrays()])
+    out = torch.empty(n, dtype=torch.float32, device=f"cuda:{local}")
+    ctx = Context(local, max_options=1)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{local}")
+    l2 = l2_bytes(local)
+    shapes = [tuple(int(x) for x in sh.split(",")) for sh in args.sweep_shapes.split(";")]
+    sizes = [int(x) for x in args.sweep_32nds.split(",")]
+    rows = []
+    for vpt, block, bps in shapes:
+        for r32 in sizes:
+            tune = (vpt, block, bps, 7 if r32 else 6, 1, r32)
+            ctx.set_tune(*tune)
+
+            def step():
+                ctx.price_soa(*dev, out, n=n, num_runs=runs, device=True, asynchronous=True)
+
+            secs, _ = time_steps(stream, step, args.steps, args.warmup)
+            per_pass = secs / (runs * args.steps)
+            t = ctx.get_tune()
+            rows.append({"tune": ",".join(str(x) for x in tune),
+                         "prefix_bytes": prefix_bytes(t, n, l2),
+                         "us_per_pass": round(per_pass * 1e6, 3),
+                         "options_per_s": n / per_pass,
+                         "frac_of_hbm": BYTES_PER_OPTION * n / per_pass / 1e9 / measured_hbm_peak()[0]})
+            print(json.dumps({"sweep_point": rows[-1]}), file=sys.stderr, flush=True)
+    best = max(rows, key=lambda r: r["options_per_s"])
+    line = {"metric": "resident-prefix sweep: options/s per (shape, prefix size)",
+            "value": best["options_per_s"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic (seeded book)",
+            "config": {"workload": f"plain map, {n} options, NUM_RUNS={runs} passes per step",
+                       "options": n, "num_runs": runs, "l2_bytes": int(l2)},
+            "best": best, "points": rows}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 # ---------------------------------------------------------- reference arm
 def run_reference(args, rank, world, local):
     """The reference's CPU path (the oracle port of its FastFlow map: same
@@ -710,11 +953,10 @@ def run_reference(args, rank, world, local):
         "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded book, reference config distributions)",
-        "config": {"workload": f"plain map, {n} European options FP32 SoA, NUM_RUNS={args.runs} "
-                               "passes per step", "options": n, "num_runs": args.runs},
+        "config": map_config(n, args.runs, world),
         "impl": "reference",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": sample},
+                         "sample": sample, "note": PORT_NOTE},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -727,13 +969,19 @@ def main(argv=None):
                     help="timed steps (default: 100 for the map, 10 otherwise)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=["map", "batch", "precision", "serve", "io", "fp64"],
+    ap.add_argument("--config", choices=["map", "batch", "precision", "serve", "io", "fp64",
+                                         "prefix-sweep"],
                     default="map")
-    ap.add_argument("--serve-rate", type=float, default=20000.0)
-    ap.add_argument("--serve-rates",
-                    default="1000,2500,5000,7500,10000,15000,20000,30000,40000,45000,50000,"
-                            "55000,60000,70000,80000,90000")
-    ap.add_argument("--serve-seconds", type=float, default=3.0)
+    ap.add_argument("--serve-rate", type=float, default=20000.0,
+                    help="serve: arrival rate of the specified trace (req/s)")
+    ap.add_argument("--serve-seconds", type=float, default=5.0,
+                    help="serve: length of the specified trace")
+    ap.add_argument("--serve-batched-rates", default="50000,55000,60000,65000,70000,75000,80000",
+                    help="serve: arrival rates of the batched loop's equal-p99 sweep")
+    ap.add_argument("--serve-plain-rates", default="1000,2500,5000,7500,10000,12500,15000",
+                    help="serve: arrival rates of the plain loop's equal-p99 sweep")
+    ap.add_argument("--serve-repeats", type=int, default=3,
+                    help="serve: traces per rate (medians are reported)")
     ap.add_argument("--serve-sizes", default="16,1048576",
                     help="serve config: request sizes log-uniform in [lo, hi] options")
     ap.add_argument("--serve-inflight", type=int, default=8)
@@ -748,8 +996,15 @@ def main(argv=None):
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 error report")
+    ap.add_argument("--no-nested", action="store_true",
+                    help="map: skip the nested 2^28, batch and serve records")
     ap.add_argument("--tune", default=None,
-                    help="vec_per_thread,block,blocks_per_sm,load_path[,pdl] instead of autotuning")
+                    help="vec_per_thread,block,blocks_per_sm,load_path[,pdl[,resident_32nds]] "
+                         "instead of autotuning")
+    ap.add_argument("--sweep-shapes", default="1,128,2;1,128,4;1,128,8;1,256,2;1,256,4;1,512,2",
+                    help="prefix-sweep: vec_per_thread,block,blocks_per_sm shapes")
+    ap.add_argument("--sweep-32nds", default="0,4,8,10,12,14,15,16,18,20,24",
+                    help="prefix-sweep: resident prefix sizes in 32nds of the L2 (0: none)")
     args = ap.parse_args(argv)
     if args.steps is None:
         args.steps = 100 if (args.config == "map" and args.impl == "ours") else 10
@@ -768,6 +1023,8 @@ def main(argv=None):
         run_io(args, rank, world, local)
     elif args.config == "fp64":
         run_fp64(args, rank, world, local)
+    elif args.config == "prefix-sweep":
+        run_prefix_sweep(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 

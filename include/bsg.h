@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define BSG_ABI_VERSION 1
+#define BSG_ABI_VERSION 2
 
 typedef struct bsg_ctx bsg_ctx;
 
@@ -189,6 +189,9 @@ int bsg_price_books_plain(bsg_ctx* ctx, const float* sptprice, const float* stri
  *    stream reaches the call when it is pinned memory).
  *  - The first call on a device looks up the scratch array's device address
  *    (cudaGetSymbolAddress); make that first call before any stream capture.
+ *    The address is kept per device together with the driver context it was
+ *    found in; after a device reset (a new primary context) the next call
+ *    looks it up again.
  *  - nseg above BSG_NOALLOC_MAX_SEGMENTS returns BSG_ERR_CAPACITY.
  *  - Every call reuses the same scratch: calls that overlap on the GPU race
  *    and give wrong prices (never writes outside their own pool).  Serialise
@@ -377,11 +380,14 @@ int bsg_write_soa(const char* path, const bsg_book* book);
 int bsg_read_soa(const char* path, bsg_book* out);
 
 /* ---- tuning ------------------------------------------------------------
- * The plain map is a family of kernels: vector width per thread, block size
- * and grid size.  bsg_autotune times the candidates on the context's device
- * for n options and makes the fastest the context's choice; the result is
- * cached in the file named by $BSG_TUNE_CACHE (if set) per (device, size
- * bucket). */
+ * The plain map is a family of kernels: vector width per thread, block size,
+ * grid size, load path and, for the resident-prefix load path, the prefix
+ * size.  bsg_autotune times the candidates on the context's device for n
+ * options and makes the fastest the context's choice: every shape over 5
+ * passes; then the prefix sizes 4..24 32nds of the L2 for the best
+ * resident-prefix shape over 25 passes; then the four fastest shapes over
+ * 25 passes twice.  The result is cached in the file named by
+ * $BSG_TUNE_CACHE (if set) per (device, size bucket). */
 typedef struct bsg_tune {
     int vec_per_thread; /* float4 groups per thread per tile: 1, 2 or 4 */
     int block;          /* threads per block: 128, 256 or 512 */
@@ -394,10 +400,12 @@ typedef struct bsg_tune {
                                grid are then fixed,
                            6 = LDG.256 evict-first (vec_per_thread 1 or 2),
                            7 = LDG.256 and STG.256 with the book's first
-                               options (15/32 of the L2 at 28 bytes each)
-                               evict-last, the rest evict-first: that
+                               options (resident_32nds of the L2 at 28 bytes
+                               each) evict-last, the rest evict-first: that
                                prefix stays in L2 across passes */
     int pdl;            /* 1 = programmatic dependent launch between passes */
+    int resident_32nds; /* load path 7: size of the resident prefix in 32nds
+                           of the device's L2, 1..24; 0 = 15 */
 } bsg_tune;
 
 int bsg_autotune(bsg_ctx* ctx, size_t n, bsg_tune* out);

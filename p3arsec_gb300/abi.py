@@ -55,7 +55,7 @@ class ErrBucket(ctypes.Structure):
 class Tune(ctypes.Structure):
     _fields_ = [("vec_per_thread", ctypes.c_int), ("block", ctypes.c_int),
                 ("blocks_per_sm", ctypes.c_int), ("load_path", ctypes.c_int),
-                ("pdl", ctypes.c_int)]
+                ("pdl", ctypes.c_int), ("resident_32nds", ctypes.c_int)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -389,8 +389,9 @@ class Context:
         _check(self.lib, self.h, self.lib.bsg_get_tune(self.h, ctypes.byref(t)))
         return t.as_dict()
 
-    def set_tune(self, vec_per_thread=1, block=256, blocks_per_sm=0, load_path=0, pdl=0):
-        t = Tune(vec_per_thread, block, blocks_per_sm, load_path, pdl)
+    def set_tune(self, vec_per_thread=1, block=256, blocks_per_sm=0, load_path=0, pdl=0,
+                 resident_32nds=0):
+        t = Tune(vec_per_thread, block, blocks_per_sm, load_path, pdl, resident_32nds)
         _check(self.lib, self.h, self.lib.bsg_set_tune(self.h, ctypes.byref(t)))
 
 

@@ -74,6 +74,44 @@ def generate(n: int, seed: int, dist: str = "plain") -> Book:
                 t.astype(f32), otype)
 
 
+def generate_device(n: int, seed: int, dist: str = "plain", device: str = "cuda:0",
+                    chunk: int = 1 << 26):
+    """Seeded book of ``n`` options drawn on the GPU (torch's Philox stream
+    ``seed``), for books too large to draw on the host in reasonable time
+    (2^28 options: seconds here against minutes with numpy).  Same field
+    distributions and float64-then-float32 rounding as :func:`generate`, a
+    different random stream.  Returns six device tensors in ``Book.arrays()``
+    order."""
+    import torch
+    if dist not in ("plain", "tails"):
+        raise ValueError(f"unknown distribution {dist!r}")
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    out = [torch.empty(n, dtype=torch.float32, device=device) for _ in range(5)]
+    ot = torch.empty(n, dtype=torch.int32, device=device)
+
+    def u(m, lo, hi):
+        return torch.rand(m, dtype=torch.float64, device=device, generator=g) * (hi - lo) + lo
+
+    for a in range(0, n, chunk):
+        m = min(chunk, n - a)
+        s = u(m, 10.0, 200.0)
+        if dist == "plain":
+            k = s * u(m, 0.5, 1.5)
+            t = u(m, 0.05, 2.0)
+        else:
+            k = s * u(m, 0.05, 20.0)
+            t = u(m, 0.001, 5.0)
+        out[0][a:a + m] = s.float()
+        out[1][a:a + m] = k.float()
+        out[4][a:a + m] = t.float()
+        del s, k, t
+        out[2][a:a + m] = u(m, 0.01, 0.10).float()
+        out[3][a:a + m] = u(m, 0.05, 0.65).float()
+        ot[a:a + m] = (torch.rand(m, device=device, generator=g) < 0.5).int()
+    return out + [ot]
+
+
 def concat(books) -> Book:
     books = list(books)
     return Book(*(np.concatenate([b.arrays()[i] for b in books]) for i in range(6)))

@@ -39,9 +39,10 @@ struct MapCfg {
     int blocks_per_sm; // 0: one block per tile; else grid = blocks_per_sm * SMs
     int load_path;     // 0: v4 nc; 1: v4 + L2 evict_first; 2: v8 (256-bit) nc;
                        // 3, 4, 5: TMA bulk copies into a shared-memory ring;
-                       // 6: v8 + L2 evict_first; 7: v8, a prefix of about
-                       // half the L2 evict_last (resident), the rest evict_first
+                       // 6: v8 + L2 evict_first; 7: v8, a prefix of the book
+                       // (res32 32nds of the L2) evict_last, the rest evict_first
     int pdl;           // 1: launch with programmatic stream serialization
+    int res32 = 15;    // LP 7: the resident prefix, in 32nds of the L2 (1..24)
 };
 
 // Accumulators of one error bucket (device scratch, zeroed per report).

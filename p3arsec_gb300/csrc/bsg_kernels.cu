@@ -7,8 +7,8 @@
 //  * SoA streams read with 128-bit (v4) or 256-bit (v8) non-coherent loads
 //    that do not allocate in L1, optionally inserted into L2 as evict_first
 //    (a cyclic scan of a working set larger than L2 then keeps a slice of it
-//    resident between passes), or with a prefix of the book (about half the
-//    L2, inputs and prices) evict_last and the rest evict_first, so that
+//    resident between passes), or with a prefix of the book (a tuned
+//    fraction of the L2, inputs and prices) evict_last and the rest evict_first, so that
 //    the prefix stays resident from pass to pass; prices stored with
 //    streaming stores (or with the prefix's policy).
 //  * Each thread loads VPT vector groups of all six arrays before computing,
@@ -44,7 +44,7 @@ struct Raw {
 // Load paths of the vector kernel: LP 0/2: ld.global.nc.L1::no_allocate
 // (v4 / v8); LP 1 / 6: the same v4 / v8 loads with an L2 evict_first cache
 // policy; LP 7: v8 loads and stores of a resident prefix of the book (the
-// first `gres` groups, sized to about half the L2) with an evict_last
+// first `gres` groups, a tuned fraction of the L2) with an evict_last
 // policy, the rest evict_first -- the prefix then stays in L2 from pass to
 // pass while the rest streams through.
 __host__ __device__ constexpr bool lp_resident(int lp) { return lp == 7; }
@@ -491,11 +491,12 @@ static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg_in
     }
     const int W = lp_v8(cfg.load_path) ? 8 : 4;
     const int64_t ngroups = n / W;
-    // LP 7: the first gres groups (15/32 of the L2 in inputs and prices,
-    // 28 bytes an option) are kept resident across passes
+    // LP 7: the first gres groups (res32 32nds of the L2 in inputs and
+    // prices, 28 bytes an option) are kept resident across passes
     int64_t gres = 0;
     if (lp_resident(cfg.load_path)) {
-        gres = device_l2_bytes() * 15 / 32 / (28 * W);
+        const int res32 = (cfg.res32 >= 1 && cfg.res32 <= 24) ? cfg.res32 : 15;
+        gres = device_l2_bytes() * res32 / 32 / (28 * W);
         if (gres > ngroups) gres = ngroups;
     }
     const int64_t tile = (int64_t)block * cfg.vpt;

@@ -42,7 +42,12 @@ static __device__ __align__(256) unsigned long long bsg_noalloc_scratch[kWords];
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
-unsigned long long* g_addr[kMaxDevices];  // device address of the scratch, per device
+// The scratch array's device address per device, and the driver context it
+// was looked up in: after a device reset the module loads again in a new
+// context and the array may sit elsewhere, so a changed context id means
+// the address is looked up again.
+unsigned long long* g_addr[kMaxDevices];
+unsigned long long g_ctx_id[kMaxDevices];
 
 // Builds the table from the raw pairs the host copied in: de-interleaves the
 // pairs, writes each segment's first tile (exclusive prefix of
@@ -197,6 +202,35 @@ bool dev_range_ok(const void* p, size_t bytes, int device) {
     return (uintptr_t)p + bytes <= end && (uintptr_t)p + bytes >= (uintptr_t)p;
 }
 
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+template <typename Fn>
+Fn driver_fn(const char* name) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion(name, &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return reinterpret_cast<Fn>(f);
+}
+
+// The unique id of the calling thread's current driver context (0 if none
+// or unknown).  The runtime calls above have made the primary context of
+// the current device current.
+unsigned long long current_ctx_id() {
+    static CtxGetCurrentFn get_cur = driver_fn<CtxGetCurrentFn>("cuCtxGetCurrent");
+    static CtxGetIdFn get_id = driver_fn<CtxGetIdFn>("cuCtxGetId");
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (!get_cur || !get_id || get_cur(&ctx) != CUDA_SUCCESS || !ctx ||
+        get_id(ctx, &id) != CUDA_SUCCESS)
+        return 0;
+    return id;
+}
+
 }  // namespace
 
 extern "C" int bsg_price_batch_noalloc(const float* sptprice, const float* strike,
@@ -229,19 +263,23 @@ extern "C" int bsg_price_batch_noalloc(const float* sptprice, const float* strik
     }
     if (ntiles == 0) return BSG_OK;
 
-    // Set-up, once per device with that device current: the device address
-    // of the scratch array (its host-side name is only a stand-in).
+    // Set-up, once per device (and again after a device reset) with that
+    // device current: the device address of the scratch array (its
+    // host-side name is only a stand-in).
     unsigned long long* scratch = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_addr[device]) {
+        const unsigned long long ctx_id = current_ctx_id();
+        if (!g_addr[device] || ctx_id == 0 || ctx_id != g_ctx_id[device]) {
             void* p = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&p, bsg_noalloc_scratch);
             if (e != cudaSuccess || !p) {
                 cudaGetLastError();
+                g_addr[device] = nullptr;
                 return BSG_ERR_CUDA;
             }
             g_addr[device] = static_cast<unsigned long long*>(p);
+            g_ctx_id[device] = ctx_id;
         }
         scratch = g_addr[device];
     }

@@ -15,8 +15,9 @@
 // every request's inputs from registered (pinned) host memory into the pool,
 // the persistent batch kernel over the requests' pool segments, and an
 // egress kernel that writes the prices to each request's host output.  No
-// per-request copy calls.  Plain path (plain = 1): one request at a time,
-// six host-to-device copies, one plain map launch, one device-to-host copy.
+// per-request copy calls.  Plain path (plain = 1): one thread prices one
+// request at a time with six host-to-device copies, one plain map launch and
+// one device-to-host copy, and completes it itself.
 #include "bsg.h"
 #include "bsg_internal.h"
 #include "bsg_math.cuh"
@@ -872,11 +873,79 @@ struct bsg_server {
         }
     }
 
+    // ------------------------------------------------------- plain path
+    // One thread takes the requests in FIFO order and prices each in turn:
+    // six copies, one plain launch, one copy back, then it polls the
+    // request's event and completes it itself.  Between requests it polls
+    // the queue for a while (as the persistent path's completer does), so
+    // neither a new request nor a finished one waits for a thread to wake
+    // from a condition variable: the baseline pays for its per-request
+    // copies and launch, not for thread hand-offs.
+    void dispatcher_plain() {
+        set_fine_timer_slack();
+        Slot& sl = slots[0];
+        std::unique_lock<std::mutex> lk(mu);
+        double last_busy = now_s();
+        bool stuck = false;  // a request overran batch_timeout: its range stays held
+        for (;;) {
+            while (!stop && (stuck || paused || queue.empty()) &&
+                   now_s() - last_busy < kPollWindow) {
+                lk.unlock();
+                std::this_thread::sleep_for(std::chrono::microseconds(2));
+                lk.lock();
+            }
+            cv_disp.wait(lk, [&] { return stop || (!stuck && !paused && !queue.empty()); });
+            if (stop) break;
+            Request* q = queue.front();
+            uint64_t off;
+            if (!pool_alloc(q->span, &off)) {  // only one request holds the pool
+                queue.pop_front();
+                complete(q, BSG_ERR_BUDGET, now_s(), false);
+                cv_done.notify_all();
+                continue;
+            }
+            queue.pop_front();
+            q->off = off;
+            q->state = Q_ADMITTED;
+            sl.reqs.assign(1, q);
+            sl.busy = true;
+            st.batches++;
+            st.max_batch_requests_seen = std::max<uint64_t>(st.max_batch_requests_seen, 1);
+            inflight.push_back(0);
+            lk.unlock();
+            int rc = enqueue_plain(sl);
+            bool release = true;
+            if (rc == BSG_OK) {
+                rc = wait_event(sl.ev);
+                release = rc != BSG_ERR_TIMEOUT;
+            } else {
+                // copies or the launch may already be enqueued: drain first
+                cudaGetLastError();
+                release = cudaStreamSynchronize(sl.st) == cudaSuccess;
+            }
+            const double t = now_s();
+            lk.lock();
+            inflight.pop_front();
+            if (rc == BSG_OK) st.kernel_launches++;
+            complete(q, rc, t, release);
+            sl.reqs.clear();
+            if (release) sl.busy = false;
+            else stuck = true;
+            free_gen++;
+            cv_done.notify_all();
+            last_busy = now_s();
+        }
+    }
+
     // ------------------------------------------------------- dispatcher
     void dispatcher() {
         cudaSetDevice(device);
         if (persistent) {
             dispatcher_persistent();
+            return;
+        }
+        if (cfg.plain) {
+            dispatcher_plain();
             return;
         }
         std::unique_lock<std::mutex> lk(mu);
@@ -960,6 +1029,7 @@ struct bsg_server {
             completer_persistent();
             return;
         }
+        if (cfg.plain) return;  // the plain path's dispatcher completes its requests
         set_fine_timer_slack();
         std::unique_lock<std::mutex> lk(mu);
         for (;;) {

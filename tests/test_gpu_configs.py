@@ -1,0 +1,70 @@
+"""GPU parity at the benchmark configurations' own sizes, against the CPU oracle.
+
+The reference checks every price against the DGrefval column at 1e-4
+(ERR_CHK, blackscholes.c:333-339).  Here the production (fast) path, called
+through the C ABI with NUM_RUNS = 100 passes as the benchmark runs it, is
+compared option by option with:
+  * oracle.price_fp64 -- the same formula in double on the float inputs:
+    max |err| <= 1e-4 (the ERR_CHK bound; no option may count as an error);
+  * oracle.price_ref -- the reference's own FP32 arithmetic (bit-identical
+    restatement): max |diff| <= 2e-4 (both sides within 1e-4 of FP64).
+Sizes: 65,536 options (the reference's usual run) and 10,000,000 options
+(the bandwidth configuration); the 2^28 and batched configurations are
+covered by the size-independent checks in test_gpu_batch.py and by the
+bench's FP64 error report.
+"""
+import numpy as np
+import pytest
+
+from p3arsec_gb300 import Context, books
+
+pytestmark = pytest.mark.gpu
+
+ERR_CHK = 1e-4  # blackscholes.c:333-339
+
+
+def _check(got, book, oracle_lib):
+    fp64 = oracle_lib.price_fp64(book)
+    err = np.abs(got.astype(np.float64) - fp64)
+    assert np.all(np.isfinite(got))
+    assert int(np.count_nonzero(err >= ERR_CHK)) == 0, (err.max(), int(np.argmax(err)))
+    ref = oracle_lib.price_ref(book).astype(np.float64)
+    assert np.abs(got.astype(np.float64) - ref).max() <= 2e-4
+    return float(err.max()), float(np.sqrt(np.mean(err * err)))
+
+
+def test_reference_size_65536_against_oracle(gpu_ctx, oracle_lib):
+    book = books.generate(65_536, seed=20241203)
+    got = gpu_ctx.price_book(book, num_runs=100, mode="fast")
+    mx, rms = _check(got, book, oracle_lib)
+    assert rms <= 2e-5, rms
+
+
+def test_bandwidth_size_10m_against_oracle(oracle_lib):
+    n = 10_000_000
+    book = books.generate(n, seed=20241203)
+    with Context(0, n) as ctx:
+        got = ctx.price_book(book, num_runs=100, mode="fast")
+    mx, rms = _check(got, book, oracle_lib)
+    assert rms <= 2e-5, rms
+
+
+def test_bandwidth_size_10m_device_pointers_every_pass_writes_the_same(oracle_lib):
+    """Device-pointer calls (the bench's timed path) over the same 10M book:
+    the 100-pass graph replay leaves the prices of a single pass."""
+    torch = pytest.importorskip("torch")
+    n = 10_000_000
+    book = books.generate(n, seed=7)
+    dev = [torch.from_numpy(a).cuda() for a in book.arrays()]
+    out = torch.full((n,), -1.0, device="cuda:0")
+    with Context(0, 1) as ctx:
+        ctx.autotune(n)
+        ctx.price_soa(*dev, out, n=n, num_runs=100, device=True)
+        torch.cuda.synchronize()
+        got100 = out.cpu().numpy()
+        out.fill_(-1.0)
+        ctx.price_soa(*dev, out, n=n, num_runs=1, device=True)
+        torch.cuda.synchronize()
+        got1 = out.cpu().numpy()
+    assert np.array_equal(got100.view(np.uint32), got1.view(np.uint32))
+    _check(got100, book, oracle_lib)

@@ -174,18 +174,22 @@ def test_all_tunings_give_identical_bits(gpu_ctx):
 
 
 def test_resident_prefix_path_on_a_book_larger_than_l2(gpu_ctx):
-    """Load path 7 keeps a prefix of the book (about half the L2) resident
-    and streams the rest: on a 4M-option book (112 MB) both parts, and the
-    boundary between them, give the bits of the plain path."""
+    """Load path 7 keeps a prefix of the book (a tuned number of 32nds of
+    the L2) resident and streams the rest: on a 4M-option book (112 MB) both
+    parts, and the boundary between them, give the bits of the plain path
+    for every prefix size the tuning accepts."""
     book = books.generate(4_000_001, seed=16)
     saved = gpu_ctx.get_tune()
     try:
         gpu_ctx.set_tune(1, 256, 0, 0, 0)
         base = gpu_ctx.price_book(book, num_runs=1)
         for vpt, block, bps, pdl in ((1, 256, 0, 1), (2, 512, 4, 1), (1, 128, 8, 0)):
-            gpu_ctx.set_tune(vpt, block, bps, 7, pdl)
-            got = gpu_ctx.price_book(book, num_runs=3)
-            assert np.array_equal(got.view(np.uint32), base.view(np.uint32)), (vpt, block, bps, pdl)
+            for r32 in (0, 1, 8, 15, 24):
+                gpu_ctx.set_tune(vpt, block, bps, 7, pdl, r32)
+                assert gpu_ctx.get_tune()["resident_32nds"] == (r32 or 15)
+                got = gpu_ctx.price_book(book, num_runs=3)
+                assert np.array_equal(got.view(np.uint32), base.view(np.uint32)), \
+                    (vpt, block, bps, pdl, r32)
     finally:
         gpu_ctx.set_tune(**saved)
 
