@@ -7,8 +7,11 @@ fallback.  Pointer arguments accept numpy arrays (host), objects with a
 """
 from __future__ import annotations
 
+import atexit
 import ctypes
 import os
+import sys
+import weakref
 
 import numpy as np
 
@@ -221,6 +224,23 @@ def _check(lib, ctx, st):
         raise BsgError(st, msg)
 
 
+# Contexts and servers still open when the interpreter exits are closed by
+# an atexit hook, while the CUDA runtime and every library that shares the
+# device are still loaded; a finaliser that runs later, during interpreter
+# teardown, leaves the handle to the process exit instead of calling into a
+# runtime that may already be shutting down.
+_live = weakref.WeakSet()
+
+
+@atexit.register
+def _close_live():
+    for obj in list(_live):
+        try:
+            obj.close()
+        except Exception:  # noqa: BLE001 -- best effort at exit
+            pass
+
+
 class Context:
     """One GPU pricing context (bsg_ctx): a device, a stream, resident buffers."""
 
@@ -233,6 +253,7 @@ class Context:
         self.h = h
         self.device = device
         self.max_options = max_options
+        _live.add(self)
 
     def close(self):
         if getattr(self, "h", None):
@@ -246,6 +267,8 @@ class Context:
         self.close()
 
     def __del__(self):
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -410,6 +433,7 @@ class Server:
         if st != 0:
             raise BsgError(st, self.lib.bsg_strerror(st).decode())
         self.h = h
+        _live.add(self)
 
     def close(self):
         if getattr(self, "h", None):

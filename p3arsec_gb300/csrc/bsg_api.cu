@@ -172,33 +172,104 @@ MemGetAddressRangeFn mem_get_address_range() {
     return fn;
 }
 
-// Checks that [p, p + bytes) lies inside one device allocation of the
-// context's device.
+typedef CUresult (*PointerGetAttributeFn)(void*, CUpointer_attribute, CUdeviceptr);
+typedef CUresult (*MemGetAccessFn)(unsigned long long*, const CUmemLocation*, CUdeviceptr);
+
+template <typename Fn>
+Fn driver_entry(const char* name) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion(name, &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return reinterpret_cast<Fn>(f);
+}
+
+// Whether the mapped piece at p was mapped through the virtual memory API
+// (cuMemCreate + cuMemMap: not usable with legacy IPC, unlike cudaMalloc
+// memory) and gives `device` read-write access.
+bool vmm_piece_rw(uintptr_t p, int device) {
+    static PointerGetAttributeFn get_attr =
+        driver_entry<PointerGetAttributeFn>("cuPointerGetAttribute");
+    static MemGetAccessFn get_access = driver_entry<MemGetAccessFn>("cuMemGetAccess");
+    if (!get_attr || !get_access) return false;
+    unsigned long long legacy_ipc = 0;  // a boolean: zero-filled whatever its width
+    if (get_attr(&legacy_ipc, CU_POINTER_ATTRIBUTE_IS_LEGACY_CUDA_IPC_CAPABLE, (CUdeviceptr)p) !=
+            CUDA_SUCCESS ||
+        legacy_ipc != 0)
+        return false;
+    CUmemLocation loc;
+    loc.type = CU_MEM_LOCATION_TYPE_DEVICE;
+    loc.id = device;
+    unsigned long long flags = 0;
+    return get_access(&flags, &loc, (CUdeviceptr)p) == CUDA_SUCCESS &&
+           flags == CU_MEM_ACCESS_FLAGS_PROT_READWRITE;
+}
+
+}  // namespace
+
+namespace bsg {
+
+int device_extent(const void* p, size_t bytes, int device) {
+    const uintptr_t want = reinterpret_cast<uintptr_t>(p) + bytes;
+    if (want < reinterpret_cast<uintptr_t>(p)) return kExtentOverrun;
+    MemGetAddressRangeFn range = mem_get_address_range();
+    if (!range) return kExtentUnknown;
+    uintptr_t cur = reinterpret_cast<uintptr_t>(p);
+    for (int piece = 0; piece < 65536; ++piece) {
+        cudaPointerAttributes attr;
+        if (cudaPointerGetAttributes(&attr, reinterpret_cast<const void*>(cur)) != cudaSuccess) {
+            cudaGetLastError();
+            return piece ? kExtentOverrun : kExtentNotDevice;
+        }
+        if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
+            return piece ? kExtentOverrun : kExtentNotDevice;
+        if (attr.type == cudaMemoryTypeDevice && attr.device != device)
+            return piece ? kExtentOverrun : kExtentOtherDevice;
+        CUdeviceptr base = 0;
+        size_t size = 0;
+        if (range(&base, &size, (CUdeviceptr)cur) != CUDA_SUCCESS)
+            return piece ? kExtentOverrun : kExtentUnknown;
+        const uintptr_t end = (uintptr_t)base + size;
+        // a piece of a virtual range must itself be readable and writable
+        // by the device; one cudaMalloc allocation is
+        const bool vmm = attr.type == cudaMemoryTypeDevice && vmm_piece_rw(cur, device);
+        if (piece && !vmm) return kExtentOverrun;
+        if (want <= end) return kExtentOk;
+        // past this piece: go on only from one mapped piece of a virtual
+        // range to the next, never from one ordinary allocation to another
+        if (!vmm) return kExtentOverrun;
+        cur = end;
+    }
+    return kExtentOverrun;
+}
+
+}  // namespace bsg
+
+namespace {
+
+// Checks that [p, p + bytes) is device memory of the context's device:
+// inside one allocation, or across consecutive mapped pieces of a virtual
+// range (bsg::device_extent).
 int check_dev_range(bsg_ctx* c, const void* p, size_t bytes, const char* name) {
     if (!p) return fail(c, BSG_ERR_INVALID_ARG, std::string(name) + " is NULL");
     if ((reinterpret_cast<uintptr_t>(p) & 3) != 0)
         return fail(c, BSG_ERR_MISALIGNED, std::string(name) + " is not 4-byte aligned");
-    cudaPointerAttributes attr;
-    cudaError_t e = cudaPointerGetAttributes(&attr, p);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return fail(c, BSG_ERR_INVALID_ARG, std::string(name) + " is not a CUDA pointer");
+    switch (bsg::device_extent(p, bytes, c->device)) {
+        case bsg::kExtentOk: return BSG_OK;
+        case bsg::kExtentNotDevice:
+            return fail(c, BSG_ERR_INVALID_ARG, std::string(name) + " is not device memory");
+        case bsg::kExtentOtherDevice:
+            return fail(c, BSG_ERR_INVALID_ARG, std::string(name) + " lives on another device");
+        case bsg::kExtentUnknown:
+            return fail(c, BSG_ERR_INVALID_ARG, std::string(name) + ": allocation range unknown");
+        default:
+            return fail(c, BSG_ERR_INVALID_ARG,
+                        std::string(name) + ": " + std::to_string(bytes) +
+                            " bytes run past the end of its allocation");
     }
-    if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
-        return fail(c, BSG_ERR_INVALID_ARG, std::string(name) + " is not device memory");
-    if (attr.type == cudaMemoryTypeDevice && attr.device != c->device)
-        return fail(c, BSG_ERR_INVALID_ARG, std::string(name) + " lives on another device");
-    CUdeviceptr base = 0;
-    size_t size = 0;
-    MemGetAddressRangeFn range = mem_get_address_range();
-    if (!range || range(&base, &size, (CUdeviceptr)p) != CUDA_SUCCESS)
-        return fail(c, BSG_ERR_INVALID_ARG, std::string(name) + ": allocation range unknown");
-    const uintptr_t end = (uintptr_t)base + size;
-    if ((uintptr_t)p + bytes > end || (uintptr_t)p + bytes < (uintptr_t)p)
-        return fail(c, BSG_ERR_INVALID_ARG,
-                    std::string(name) + ": " + std::to_string(bytes) +
-                        " bytes run past the end of its allocation");
-    return BSG_OK;
 }
 
 int check_soa_dev(bsg_ctx* c, const bsg::SoA& a, size_t n, size_t out_elem) {

@@ -117,6 +117,21 @@ struct NvtxRange {
     NvtxRange& operator=(const NvtxRange&) = delete;
 };
 
+// Where [p, p + bytes) lies: kExtentOk when it is device memory of `device`
+// (or managed memory) inside one allocation, or across consecutive pieces
+// that the virtual memory API mapped into one range with read-write access
+// for `device` (pool allocators that grow in place map memory piece by
+// piece).  Ordinary allocations are never joined with their neighbours, so
+// a size that runs past one is kExtentOverrun.
+enum Extent : int {
+    kExtentOk = 0,
+    kExtentNotDevice = 1,
+    kExtentOtherDevice = 2,
+    kExtentUnknown = 3,
+    kExtentOverrun = 4,
+};
+int device_extent(const void* p, size_t bytes, int device);
+
 // Fills n options with a deterministic plausible book (autotuning input).
 cudaError_t launch_fill(const SoA& a, int64_t n, uint32_t seed, int sm_count,
                         cudaStream_t st);

@@ -167,39 +167,11 @@ __global__ void __launch_bounds__(kBlock) noalloc_batch_kernel(
     }
 }
 
-typedef CUresult (*RangeFn)(CUdeviceptr*, size_t*, CUdeviceptr);
-
-RangeFn range_fn() {
-    static RangeFn fn = [] {
-        void* f = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuMemGetAddressRange", &f, 12000,
-                                             cudaEnableDefault, &q) != cudaSuccess ||
-            q != cudaDriverEntryPointSuccess) {
-            cudaGetLastError();
-            f = nullptr;
-        }
-        return reinterpret_cast<RangeFn>(f);
-    }();
-    return fn;
-}
-
-// [p, p + bytes) inside one device allocation of `device`, 16-byte aligned.
+// [p, p + bytes) device memory of `device` (one allocation, or consecutive
+// mapped pieces of a virtual range), 16-byte aligned.
 bool dev_range_ok(const void* p, size_t bytes, int device) {
     if (!p || (reinterpret_cast<uintptr_t>(p) & 15)) return false;
-    cudaPointerAttributes a;
-    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-        cudaGetLastError();
-        return false;
-    }
-    if (a.type == cudaMemoryTypeDevice && a.device != device) return false;
-    if (a.type != cudaMemoryTypeDevice && a.type != cudaMemoryTypeManaged) return false;
-    RangeFn fn = range_fn();
-    CUdeviceptr base = 0;
-    size_t size = 0;
-    if (!fn || fn(&base, &size, (CUdeviceptr)p) != CUDA_SUCCESS) return false;
-    const uintptr_t end = (uintptr_t)base + size;
-    return (uintptr_t)p + bytes <= end && (uintptr_t)p + bytes >= (uintptr_t)p;
+    return bsg::device_extent(p, bytes, device) == bsg::kExtentOk;
 }
 
 typedef CUresult (*CtxGetCurrentFn)(CUcontext*);

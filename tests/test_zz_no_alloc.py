@@ -120,7 +120,9 @@ _EXPANDABLE = textwrap.dedent("""
         ctx.price_batch(pool, want, n, segs)
     torch.cuda.synchronize()
     same = torch.equal(got.view(torch.int32), want.view(torch.int32))
-    print("STATUS", st, "SAME", int(same))
+    # a size far past the mapped pieces is still refused
+    over = abi.price_batch_noalloc(pool, got, 1 << 35, [(0, 1)])
+    print("STATUS", st, "SAME", int(same), "OVER", over)
 """)
 
 
@@ -132,7 +134,7 @@ def test_noalloc_on_a_pool_mapped_piece_by_piece():
     r = subprocess.run([sys.executable, "-c", _EXPANDABLE.format(root=ROOT)], cwd=ROOT, env=env,
                        stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=300)
     assert r.returncode == 0, r.stderr[-3000:]
-    assert "STATUS 0 SAME 1" in r.stdout, r.stdout + r.stderr[-3000:]
+    assert "STATUS 0 SAME 1 OVER -1" in r.stdout, r.stdout + r.stderr[-3000:]
 
 
 def test_noalloc_rejects_more_segments_than_its_scratch(gpu_ctx):
