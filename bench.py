@@ -18,7 +18,7 @@ records measured in the same run:
   under p99 bounds of 0.5, 1 and 2 ms (medians of repeated traces).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--config map|batch|precision|serve|io|fp64|prefix-sweep]
+                    [--config map|batch|precision|serve|io|fp64|prefix-sweep|swaptions]
 
 One JSON line on stdout (rank 0).  Under torchrun each rank prices its own
 book on its own GPU (weak scaling, no collective on the data path); the
@@ -870,6 +870,71 @@ def run_io(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
+# --------------------------------------------------------------- swaptions
+def run_swaptions(args, rank, world, local):
+    """The swaptions application (P3ARSEC's HJM Monte Carlo,
+    HJM_Swaption_Blocking.cpp): args.swaptions swaptions of the reference
+    driver's kind, args.trials paths each, priced in one call of
+    bsg_price_swaptions; the CPU oracle (the same model and random stream,
+    the whole path matrix as the reference simulates it) on every host core
+    over a bounded sample is the CPU baseline, and the GPU's prices on that
+    sample are checked against it."""
+    import torch
+
+    import oracle
+    from p3arsec_gb300 import Context
+    from p3arsec_gb300 import build as b
+    from p3arsec_gb300 import swaptions as S
+    b.build()
+    oracle.build(ref=False)
+    torch.cuda.set_device(local)
+    sw = S.generate(args.swaptions, seed=1979)
+    ctx = Context(local, max_options=1)
+    trials = args.trials
+    for _ in range(args.warmup):
+        ctx.price_swaptions(sw, trials)
+    l0 = ctx.launches
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            price, err = ctx.price_swaptions(sw, trials)
+            times.append(time.perf_counter() - t0)
+    launches = ctx.launches - l0
+    secs = float(np.median(times))
+    paths = len(sw) * trials
+    # the same swaptions on a sample of the trials, GPU and CPU oracle
+    sample = min(trials, args.swaption_sample)
+    g_s, g_e = ctx.price_swaptions(sw, sample)
+    threads = os.cpu_count() or 1
+    c_s, c_e, c_secs = oracle.swaptions_all(sw, sample, threads)
+    rel = float(np.max(np.abs(g_s - c_s) / np.maximum(np.abs(c_s), 1e-12)))
+    line = {
+        "metric": "swaption paths/s (HJM Monte Carlo, FP64)",
+        "value": paths / secs, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * secs, "higher_is_better": True,
+        "dtype": "f64", "data": "synthetic (the reference driver's swaption set, seeded)",
+        "config": {"workload": f"{len(sw)} swaptions x {trials} paths, 11-point HJM grid, "
+                               "3 factors, one bsg_price_swaptions call per step (host arrays in, "
+                               "prices out)", "swaptions": len(sw), "trials": trials},
+        "step_time_s": {"median": secs, "min": min(times), "max": max(times)},
+        "prices": {"first": price[:4].tolist(), "std_err_first": err[:4].tolist()},
+        "gpu_launches": launches,
+        "vs_oracle": {"sample_trials": sample, "max_rel_price_diff": rel,
+                      "note": "the same paths on the CPU oracle; parity with the reference "
+                              "itself is unpinned (its model core is not in its tree)"},
+        "cpu_baseline": {"value": len(sw) * sample / c_secs, "unit": "paths/s",
+                         "cores": threads, "kind": "port",
+                         "sample": f"{len(sw)} swaptions x {sample} paths, static partition over "
+                                   f"{threads} threads, {c_secs:.2f} s (the oracle simulates every "
+                                   "row of each path, as the reference does)"},
+        "clocks": clk.summary(),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 # ---------------------------------------------------- resident-prefix sweep
 def run_prefix_sweep(args, rank, world, local):
     """The map over one book for every (shape, resident prefix size): the
@@ -970,7 +1035,7 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", choices=["map", "batch", "precision", "serve", "io", "fp64",
-                                         "prefix-sweep"],
+                                         "prefix-sweep", "swaptions"],
                     default="map")
     ap.add_argument("--serve-rate", type=float, default=20000.0,
                     help="serve: arrival rate of the specified trace (req/s)")
@@ -996,6 +1061,12 @@ def main(argv=None):
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 error report")
+    ap.add_argument("--swaptions", type=int, default=128,
+                    help="swaptions config: number of swaptions")
+    ap.add_argument("--trials", type=int, default=1_000_000,
+                    help="swaptions config: Monte Carlo paths per swaption")
+    ap.add_argument("--swaption-sample", type=int, default=200_000,
+                    help="swaptions config: paths per swaption of the CPU-oracle sample")
     ap.add_argument("--no-nested", action="store_true",
                     help="map: skip the nested 2^28, batch and serve records")
     ap.add_argument("--tune", default=None,
@@ -1025,6 +1096,8 @@ def main(argv=None):
         run_fp64(args, rank, world, local)
     elif args.config == "prefix-sweep":
         run_prefix_sweep(args, rank, world, local)
+    elif args.config == "swaptions":
+        run_swaptions(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 

@@ -345,6 +345,53 @@ typedef struct bsg_trace_result {
 int bsg_serve_trace(const bsg_server_config* cfg, const bsg_trace_config* trace,
                     bsg_trace_result* out, double* latencies_out, size_t latencies_cap);
 
+/* ---- swaptions (HJM Monte Carlo) --------------------------------------
+ * P3ARSEC's swaptions application: each swaption priced by Monte Carlo
+ * simulation of forward-rate paths under a multi-factor HJM model
+ * (parsec-ff/pkgs/apps/swaptions/src/HJM_Swaption_Blocking.cpp:19-223),
+ * one swaption per iteration of a FastFlow ParallelFor
+ * (HJM_Securities.cpp:312-323).  The reference tree holds the driver but
+ * not the model core, so the model here is the published discrete HJM
+ * model (time-to-maturity parameterisation, the drift that makes
+ * discounted bonds martingales) and the paths' variates come from a
+ * counter-based generator keyed by (seed, trial): prices agree with the
+ * reference's in distribution, not trial for trial.  Double precision
+ * throughout, as the reference's FTYPE. */
+typedef struct bsg_swaption {
+    double strike;           /* dStrike */
+    double compounding;      /* dCompounding: 0 = the strike is continuously compounded */
+    double maturity;         /* dMaturity: years to the option's expiry */
+    double tenor;            /* dTenor: years of the underlying swap */
+    double payment_interval; /* dPaymentInterval: years between swap payments */
+    double years;            /* dYears: horizon of the HJM grid */
+    int n_steps;             /* iN: grid points, 2..32 */
+    int n_factors;           /* iFactors: volatility factors, 1..8 */
+    const double* yield;     /* n_steps continuously compounded yields */
+    const double* factors;   /* n_factors x (n_steps - 1) vols, row-major: factor
+                                k's vol of the forward m + 1 steps from maturity */
+    uint64_t seed;           /* the paths' random stream (iRndSeed) */
+} bsg_swaption;
+
+/* Prices n swaptions with `trials` paths each (2..2^40) in one launch:
+ * price[i] = mean discounted payoff max(V - 1, 0) D, std_err[i] (optional)
+ * = its standard error, both as the reference computes them
+ * (HJM_Swaption_Blocking.cpp:191-214).  Host arrays; the call returns when
+ * the results are in.  Deterministic: the same inputs give the same bits.
+ * BSG_ERR_INVALID_ARG names the first swaption whose maturity, tenor or
+ * payment interval does not fit its grid. */
+int bsg_price_swaptions(bsg_ctx* ctx, const bsg_swaption* swaptions, size_t n,
+                        uint64_t trials, double* price, double* std_err);
+
+/* The reference's per-swaption signature (HJM_Swaption_Blocking.cpp:19-41;
+ * FTYPE = double) on the default context of device 0: pdSwaptionPrice[0] =
+ * price, [1] = standard error.  Returns 1 on success as the reference does,
+ * else a bsg_status.  BLOCKSIZE and tid are accepted and unused. */
+int bsg_HJM_Swaption_Blocking(double* pdSwaptionPrice, double dStrike, double dCompounding,
+                              double dMaturity, double dTenor, double dPaymentInterval,
+                              int iN, int iFactors, double dYears, double* pdYield,
+                              double** ppdFactors, long iRndSeed, long lTrials,
+                              int BLOCKSIZE, int tid);
+
 /* ---- the reference's file formats (host code) --------------------------
  * Input, blackscholes.c:695-739: a count ("%i"), then per option
  * "%f %f %f %f %f %f %c %f %f" = s strike r divq v t OptionType divs

@@ -218,3 +218,87 @@ def bs_map(book, nthreads: int, num_runs: int):
     if secs < 0:
         raise RuntimeError("bso_bs_map failed")
     return out, secs
+
+
+# ---------------------------------------------------------------- swaptions
+class SwoSwaption(ctypes.Structure):
+    """swo_swaption (swpt_oracle.h)."""
+    _fields_ = [("strike", ctypes.c_double), ("compounding", ctypes.c_double),
+                ("maturity", ctypes.c_double), ("tenor", ctypes.c_double),
+                ("payment_interval", ctypes.c_double), ("years", ctypes.c_double),
+                ("n_steps", ctypes.c_int), ("n_factors", ctypes.c_int),
+                ("yield_", _P), ("factors", _P), ("seed", ctypes.c_uint64)]
+
+
+def _swo_lib():
+    L = lib()
+    if not getattr(L, "_swo_ready", False):
+        L.swo_price.restype = ctypes.c_int
+        L.swo_price.argtypes = [ctypes.POINTER(SwoSwaption), ctypes.c_uint64, ctypes.c_uint,
+                                ctypes.POINTER(ctypes.c_double)]
+        L.swo_price_all.restype = ctypes.c_double
+        L.swo_price_all.argtypes = [ctypes.POINTER(SwoSwaption), ctypes.c_int, ctypes.c_uint64,
+                                    ctypes.c_int, _P, _P]
+        L.swo_normal_pair.restype = None
+        L.swo_normal_pair.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32,
+                                      ctypes.POINTER(ctypes.c_double)]
+        L.swo_yield_to_forward.restype = None
+        L.swo_yield_to_forward.argtypes = [ctypes.c_int, _P, _P]
+        L.swo_drift.restype = None
+        L.swo_drift.argtypes = [ctypes.c_int, ctypes.c_int, _P, ctypes.c_double, _P]
+        L._swo_ready = True
+    return L
+
+
+def _swo_structs(swaptions):
+    keep, arr = [], (SwoSwaption * max(len(swaptions), 1))()
+    for i, s in enumerate(swaptions):
+        y = np.ascontiguousarray(s.yield_curve, dtype=np.float64)
+        f = np.ascontiguousarray(s.factors, dtype=np.float64)
+        keep += [y, f]
+        arr[i] = SwoSwaption(s.strike, s.compounding, s.maturity, s.tenor, s.payment_interval,
+                             s.years, s.n_steps, s.n_factors, _p(y), _p(f), s.seed)
+    return arr, keep
+
+
+def swaption_price(swaption, trials: int, unfloored: bool = False):
+    """(mean, standard error) of one swaption over `trials` paths; the whole
+    HJM path matrix is simulated, as the reference does."""
+    arr, keep = _swo_structs([swaption])
+    out = (ctypes.c_double * 2)()
+    if _swo_lib().swo_price(arr, trials, 1 if unfloored else 0, out) != 1:
+        raise ValueError("swaption parameters out of the reference's range")
+    return out[0], out[1]
+
+
+def swaptions_all(swaptions, trials: int, nthreads: int):
+    """Every swaption on nthreads threads (static partition, as the reference's
+    ParallelFor); returns (prices, standard errors, wall seconds)."""
+    arr, keep = _swo_structs(swaptions)
+    n = len(swaptions)
+    price = np.empty(n)
+    err = np.empty(n)
+    secs = _swo_lib().swo_price_all(arr, n, trials, nthreads, _p(price), _p(err))
+    if secs < 0:
+        raise ValueError("swaption parameters out of the reference's range")
+    return price, err, secs
+
+
+def normal_pair(seed: int, trial: int, j: int):
+    z = (ctypes.c_double * 2)()
+    _swo_lib().swo_normal_pair(seed, trial, j, z)
+    return z[0], z[1]
+
+
+def yield_to_forward(y):
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    f = np.empty_like(y)
+    _swo_lib().swo_yield_to_forward(len(y), _p(y), _p(f))
+    return f
+
+
+def hjm_drift(factors, h: float):
+    v = np.ascontiguousarray(factors, dtype=np.float64)
+    mu = np.empty(v.shape[1])
+    _swo_lib().swo_drift(v.shape[1] + 1, v.shape[0], _p(v), h, _p(mu))
+    return mu

@@ -128,6 +128,16 @@ class BatchTune(ctypes.Structure):
         return {"tile_options": int(self.tile_options), "blocks_per_sm": int(self.blocks_per_sm)}
 
 
+class SwaptionC(ctypes.Structure):
+    """bsg_swaption (include/bsg.h)."""
+    _fields_ = [("strike", ctypes.c_double), ("compounding", ctypes.c_double),
+                ("maturity", ctypes.c_double), ("tenor", ctypes.c_double),
+                ("payment_interval", ctypes.c_double), ("years", ctypes.c_double),
+                ("n_steps", ctypes.c_int), ("n_factors", ctypes.c_int),
+                ("yield_", ctypes.c_void_p), ("factors", ctypes.c_void_p),
+                ("seed", ctypes.c_uint64)]
+
+
 # Every symbol the header declares, with its ctypes signature.
 _P = ctypes.c_void_p
 _SZ = ctypes.c_size_t
@@ -180,6 +190,10 @@ SIGNATURES = {
     "bsg_selftest_guard": (_I, [_P]),
     "bsg_get_tune": (_I, [_P, ctypes.POINTER(Tune)]),
     "bsg_set_tune": (_I, [_P, ctypes.POINTER(Tune)]),
+    "bsg_price_swaptions": (_I, [_P, ctypes.POINTER(SwaptionC), _SZ, ctypes.c_uint64, _P, _P]),
+    "bsg_HJM_Swaption_Blocking": (_I, [_P] + [ctypes.c_double] * 5 + [_I, _I, ctypes.c_double,
+                                                                       _P, _P, ctypes.c_long,
+                                                                       ctypes.c_long, _I, _I]),
 }
 
 _lib = None
@@ -412,6 +426,18 @@ class Context:
         _check(self.lib, self.h, self.lib.bsg_get_tune(self.h, ctypes.byref(t)))
         return t.as_dict()
 
+    # ---------------------------------------------------------- swaptions
+    def price_swaptions(self, swaptions, trials: int):
+        """bsg_price_swaptions over p3arsec_gb300.swaptions.Swaption objects;
+        returns (prices, standard errors) as float64 arrays."""
+        arr, keep = swaption_structs(swaptions)
+        n = len(swaptions)
+        price = np.empty(n)
+        err = np.empty(n)
+        st = self.lib.bsg_price_swaptions(self.h, arr, n, trials, ptr(price), ptr(err))
+        _check(self.lib, self.h, st)
+        return price, err
+
     def set_tune(self, vec_per_thread=1, block=256, blocks_per_sm=0, load_path=0, pdl=0,
                  resident_32nds=0):
         t = Tune(vec_per_thread, block, blocks_per_sm, load_path, pdl, resident_32nds)
@@ -499,6 +525,34 @@ def serve_trace(host_pool, prices, rate_per_s, duration_s, min_n=16, max_n=1 << 
     if st != 0:
         raise BsgError(st, lib.bsg_strerror(st).decode())
     return res.as_dict()
+
+
+def swaption_structs(swaptions):
+    """bsg_swaption array for p3arsec_gb300.swaptions.Swaption objects, and the
+    numpy arrays it points into (keep them alive while the array is used)."""
+    keep, arr = [], (SwaptionC * max(len(swaptions), 1))()
+    for i, w in enumerate(swaptions):
+        y = np.ascontiguousarray(w.yield_curve, dtype=np.float64)
+        f = np.ascontiguousarray(w.factors, dtype=np.float64)
+        keep += [y, f]
+        arr[i] = SwaptionC(w.strike, w.compounding, w.maturity, w.tenor, w.payment_interval,
+                           w.years, w.n_steps, w.n_factors, y.ctypes.data, f.ctypes.data, w.seed)
+    return arr, keep
+
+
+def HJM_Swaption_Blocking(w, trials: int):
+    """The reference's per-swaption call shape (bsg_HJM_Swaption_Blocking):
+    returns (status, price, standard error); status 1 = success."""
+    lib = load()
+    y = np.ascontiguousarray(w.yield_curve, dtype=np.float64)
+    rows = [np.ascontiguousarray(r, dtype=np.float64) for r in w.factors]
+    pp = (ctypes.c_void_p * len(rows))(*[r.ctypes.data for r in rows])
+    out = np.zeros(2)
+    st = lib.bsg_HJM_Swaption_Blocking(ptr(out), w.strike, w.compounding, w.maturity, w.tenor,
+                                       w.payment_interval, w.n_steps, w.n_factors, w.years,
+                                       ptr(y), ctypes.cast(pp, ctypes.c_void_p), w.seed, trials,
+                                       16, 0)
+    return st, float(out[0]), float(out[1])
 
 
 NOALLOC_MAX_SEGMENTS = 4096

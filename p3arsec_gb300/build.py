@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-Wall", "-I" + os.path.join(ROOT, "include"),
                      "-I" + CSRC]
-CU_SOURCES = ["bsg_kernels.cu", "bsg_api.cu", "bsg_serve.cu", "bsg_noalloc.cu"]
+CU_SOURCES = ["bsg_kernels.cu", "bsg_api.cu", "bsg_serve.cu", "bsg_noalloc.cu", "bsg_swaptions.cu"]
 CPP_SOURCES = ["bsg_io.cpp"]  # host code, compiled with g++
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-Wall", "-pthread",
              "-I" + os.path.join(ROOT, "include")]

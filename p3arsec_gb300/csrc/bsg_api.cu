@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -118,6 +119,9 @@ struct bsg_ctx {
     // each synchronous call; d_guard holds the check's {count, first index}
     bool debug = false;
     unsigned long long* d_guard = nullptr;
+    // swaption scratch: parameter table, per-block partial sums, results
+    char* d_sw = nullptr;
+    size_t sw_cap = 0;
 
     bsg::SoA resident(size_t n, int set = 0) const {
         (void)n;
@@ -649,6 +653,7 @@ void bsg_destroy(bsg_ctx* c) {
     if (c->d_acc) cudaFree(c->d_acc);
     if (c->d_edges) cudaFree(c->d_edges);
     if (c->d_guard) cudaFree(c->d_guard);
+    if (c->d_sw) cudaFree(c->d_sw);
     if (c->seg_ev) cudaEventDestroy(c->seg_ev);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -1158,6 +1163,135 @@ int bsg_set_tune(bsg_ctx* c, const bsg_tune* t) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------- swaptions
+// The driver's per-swaption constants, rounded as the reference rounds them
+// (HJM_Swaption_Blocking.cpp:48-62, 116-127), checked so that every index
+// the kernel uses stays inside the path and the payment vector (the
+// reference would write past its payment vector when the tenor reaches past
+// the path).  Returns an empty string when the swaption is valid.
+static std::string swaption_setup(const bsg_swaption& w, bsg::SwParams* p) {
+    const int n = w.n_steps, nf = w.n_factors;
+    if (n < 2 || n > bsg::kSwMaxSteps) return "n_steps must be 2.." + std::to_string(bsg::kSwMaxSteps);
+    if (nf < 1 || nf > bsg::kSwMaxFactors)
+        return "n_factors must be 1.." + std::to_string(bsg::kSwMaxFactors);
+    if (!w.yield || !w.factors) return "yield or factors is NULL";
+    if (!(w.years > 0) || !(w.maturity > 0) || !(w.tenor > 0) || !(w.payment_interval > 0) ||
+        !(w.compounding >= 0))
+        return "years, maturity, tenor and payment_interval must be > 0, compounding >= 0";
+    std::memset(p, 0, sizeof(*p));
+    p->h = w.years / n;
+    p->sqh = std::sqrt(p->h);
+    p->freq = (int)(w.payment_interval / p->h + 0.5);
+    p->strike_cont = w.compounding == 0 ? w.strike
+                                        : (1 / w.compounding) * std::log(1 + w.strike * w.compounding);
+    p->swap_len = (int)(n - w.maturity / p->h + 0.5);
+    p->start = (int)(w.maturity / p->h + 0.5);
+    p->swap_points = (int)(w.tenor / p->h + 0.5);
+    p->payment_interval = w.payment_interval;
+    p->n_steps = n;
+    p->n_factors = nf;
+    p->seed = w.seed;
+    if (p->freq < 1 || p->start < 1 || p->start > n - 1 || p->swap_len < 1 ||
+        p->swap_len > n - p->start || p->swap_points >= p->swap_len)
+        return "maturity, tenor and payment interval do not fit the grid of n_steps points over years";
+    for (int i = 0; i < n; ++i) {
+        p->yield[i] = w.yield[i];
+        if (!std::isfinite(w.yield[i])) return "yield is not finite";
+    }
+    for (int k = 0; k < nf; ++k)
+        for (int m = 0; m < n - 1; ++m) {
+            p->vol[k][m] = w.factors[(size_t)k * (n - 1) + m];
+            if (!std::isfinite(p->vol[k][m])) return "factors are not finite";
+        }
+    if (!std::isfinite(p->strike_cont)) return "strike is not finite";
+    return std::string();
+}
+
+extern "C" int bsg_price_swaptions(bsg_ctx* c, const bsg_swaption* sw, size_t n, uint64_t trials,
+                                   double* price, double* std_err) {
+    if (!c) return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mu);
+    bsg::NvtxRange nvtx_("bsg_price_swaptions");
+    if (n == 0) return BSG_OK;
+    if (!sw || !price) return fail(c, BSG_ERR_INVALID_ARG, "swaptions or price is NULL");
+    if (n > 65535) return fail(c, BSG_ERR_CAPACITY, "at most 65535 swaptions per call");
+    if (trials < 2 || trials > ((uint64_t)1 << 40))
+        return fail(c, BSG_ERR_INVALID_ARG, "trials must be 2..2^40");
+    std::vector<bsg::SwParams> tab(n);
+    int max_steps = 2;
+    for (size_t i = 0; i < n; ++i) {
+        const std::string why = swaption_setup(sw[i], &tab[i]);
+        if (!why.empty()) return fail(c, BSG_ERR_INVALID_ARG, "swaption " + std::to_string(i) + ": " + why);
+        max_steps = std::max(max_steps, sw[i].n_steps);
+    }
+    BSG_CK(c, cudaSetDevice(c->device));
+    if (int st = drain_pipeline(c)) return st;
+    const int per_thread = 4;
+    const size_t chunks = (size_t)bsg::swaption_chunks(trials, per_thread);
+    const size_t tab_b = round_up(n * sizeof(bsg::SwParams), 256);
+    const size_t part_b = round_up(2 * n * chunks * sizeof(double), 256);
+    const size_t out_b = round_up(2 * n * sizeof(double), 256);
+    const size_t need = tab_b + part_b + out_b;
+    if (need > c->sw_cap) {
+        if (c->d_sw) {
+            BSG_CK(c, cudaStreamSynchronize(c->stream));
+            cudaFree(c->d_sw);
+            c->d_sw = nullptr;
+            c->sw_cap = 0;
+        }
+        if (cudaMalloc(&c->d_sw, need) != cudaSuccess) {
+            cudaGetLastError();
+            return fail(c, BSG_ERR_OUT_OF_MEMORY, "swaption scratch");
+        }
+        c->sw_cap = need;
+    }
+    bsg::SwParams* d_tab = reinterpret_cast<bsg::SwParams*>(c->d_sw);
+    double* d_part = reinterpret_cast<double*>(c->d_sw + tab_b);
+    double* d_out = reinterpret_cast<double*>(c->d_sw + tab_b + part_b);
+    BSG_CK(c, cudaMemcpyAsync(d_tab, tab.data(), n * sizeof(bsg::SwParams), cudaMemcpyHostToDevice,
+                              c->stream));
+    cudaError_t e = bsg::launch_swaptions(d_tab, (int)n, max_steps, trials, per_thread, d_part, d_out,
+                                          c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "launch_swaptions");
+    c->launches += 2;
+    std::vector<double> out(2 * n);
+    BSG_CK(c, cudaMemcpyAsync(out.data(), d_out, 2 * n * sizeof(double), cudaMemcpyDeviceToHost,
+                              c->stream));
+    BSG_CK(c, cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i < n; ++i) {
+        price[i] = out[2 * i];
+        if (std_err) std_err[i] = out[2 * i + 1];
+    }
+    return BSG_OK;
+}
+
+extern "C" int bsg_HJM_Swaption_Blocking(double* pdSwaptionPrice, double dStrike,
+                                         double dCompounding, double dMaturity, double dTenor,
+                                         double dPaymentInterval, int iN, int iFactors,
+                                         double dYears, double* pdYield, double** ppdFactors,
+                                         long iRndSeed, long lTrials, int BLOCKSIZE, int tid) {
+    (void)BLOCKSIZE;  // the GPU's blocking is its own
+    (void)tid;
+    if (!pdSwaptionPrice || !ppdFactors || iFactors < 1 || iFactors > bsg::kSwMaxFactors ||
+        iN < 2 || iN > bsg::kSwMaxSteps || lTrials < 2)
+        return BSG_ERR_INVALID_ARG;
+    double vol[bsg::kSwMaxFactors * bsg::kSwMaxSteps];
+    for (int k = 0; k < iFactors; ++k) {
+        if (!ppdFactors[k]) return BSG_ERR_INVALID_ARG;
+        for (int m = 0; m < iN - 1; ++m) vol[k * (iN - 1) + m] = ppdFactors[k][m];
+    }
+    const bsg_swaption w{dStrike, dCompounding, dMaturity, dTenor, dPaymentInterval, dYears,
+                         iN, iFactors, pdYield, vol, (uint64_t)iRndSeed};
+    std::lock_guard<std::mutex> lk(g_default_mu);
+    if (!g_default) {
+        int st = bsg_create(&g_default, 0, (size_t)1 << 16);
+        if (st) return st;
+    }
+    const int st = bsg_price_swaptions(g_default, &w, 1, (uint64_t)lTrials, &pdSwaptionPrice[0],
+                                       &pdSwaptionPrice[1]);
+    return st == BSG_OK ? 1 : st;
+}
 
 // ------------------------------------------------------------- autotuner
 // Times every plain-map shape on the context's device for n options and

@@ -132,6 +132,34 @@ enum Extent : int {
 };
 int device_extent(const void* p, size_t bytes, int device);
 
+// ---- swaptions (HJM Monte Carlo) -------------------------------------------
+constexpr int kSwMaxSteps = 32;    // grid points of the HJM path (iN)
+constexpr int kSwMaxFactors = 8;   // volatility factors (iFactors)
+
+// One swaption as the path kernel reads it: the driver's constants, already
+// rounded as the reference rounds them, and the raw curves.
+struct SwParams {
+    double strike_cont;       // strike in continuous compounding
+    double payment_interval;  // years between swap payments
+    double h, sqh;            // grid step and its square root
+    int n_steps, n_factors;
+    int start;                // the swaption's maturity on the grid
+    int swap_len;             // forward rates of the swap curve at maturity
+    int freq, swap_points;    // payment every freq steps, the last at swap_points
+    uint64_t seed;            // the paths' random stream
+    double yield[kSwMaxSteps];
+    double vol[kSwMaxFactors][kSwMaxSteps];  // [k][m], m < n_steps - 1
+};
+
+// Blocks of trials per swaption for `trials` paths, per_thread paths per thread.
+int swaption_chunks(uint64_t trials, int per_thread);
+// Prices nsw swaptions (device table prm) with `trials` paths each:
+// out[2 i] = mean discounted payoff, out[2 i + 1] = its standard error.
+// partial: device scratch of 2 * nsw * swaption_chunks(trials, per_thread)
+// doubles.  max_steps: the largest n_steps in the table.
+cudaError_t launch_swaptions(const SwParams* prm, int nsw, int max_steps, uint64_t trials,
+                             int per_thread, double* partial, double* out, cudaStream_t st);
+
 // Fills n options with a deterministic plausible book (autotuning input).
 cudaError_t launch_fill(const SoA& a, int64_t n, uint32_t seed, int sm_count,
                         cudaStream_t st);
