@@ -449,7 +449,12 @@ typedef struct bsg_tune {
                            7 = LDG.256 and STG.256 with the book's first
                                options (resident_32nds of the L2 at 28 bytes
                                each) evict-last, the rest evict-first: that
-                               prefix stays in L2 across passes */
+                               prefix stays in L2 across passes,
+                           8 = LDG.256 and STG.256 with the default L2
+                               policy, every other pass walking the book
+                               from its last tile to its first: each pass
+                               starts on the lines the previous one touched
+                               last (vec_per_thread 1 or 2) */
     int pdl;            /* 1 = programmatic dependent launch between passes */
     int resident_32nds; /* load path 7: size of the resident prefix in 32nds
                            of the device's L2, 1..24; 0 = 15 */

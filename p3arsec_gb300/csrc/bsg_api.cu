@@ -1143,7 +1143,7 @@ static bool tune_valid(const bsg_tune* t) {
                         (t->vec_per_thread == 4 && t->load_path < 2);
     const bool blk_ok = t->block == 128 || t->block == 256 || t->block == 512;
     return vpt_ok && blk_ok && t->blocks_per_sm >= 0 && t->blocks_per_sm <= 64 &&
-           t->load_path >= 0 && t->load_path <= 7 && (t->pdl == 0 || t->pdl == 1) &&
+           t->load_path >= 0 && t->load_path <= 8 && (t->pdl == 0 || t->pdl == 1) &&
            t->resident_32nds >= 0 && t->resident_32nds <= 24;
 }
 
@@ -1393,7 +1393,7 @@ extern "C" int bsg_autotune(bsg_ctx* c, size_t n, bsg_tune* out) {
     };
     // stage 1: every shape for 5 passes (the resident prefix at 15/32)
     std::vector<std::pair<float, bsg_tune>> timed;
-    for (int lp : {0, 1, 2, 6, 7})
+    for (int lp : {0, 1, 2, 6, 7, 8})
         for (int vpt : {1, 2, 4})
             for (int block : {128, 256, 512})
                 for (int bps : {0, 2, 4, 8})

@@ -40,9 +40,11 @@ struct MapCfg {
     int load_path;     // 0: v4 nc; 1: v4 + L2 evict_first; 2: v8 (256-bit) nc;
                        // 3, 4, 5: TMA bulk copies into a shared-memory ring;
                        // 6: v8 + L2 evict_first; 7: v8, a prefix of the book
-                       // (res32 32nds of the L2) evict_last, the rest evict_first
+                       // (res32 32nds of the L2) evict_last, the rest evict_first;
+                       // 8: v8, every other pass in reverse tile order
     int pdl;           // 1: launch with programmatic stream serialization
     int res32 = 15;    // LP 7: the resident prefix, in 32nds of the L2 (1..24)
+    int rev = 0;       // LP 8: this pass walks the tiles from the last to the first
 };
 
 // Accumulators of one error bucket (device scratch, zeroed per report).
@@ -68,8 +70,12 @@ cudaError_t launch_map(const SoA& a, int64_t n, int mode, const MapCfg& cfg,
 // evict_first (6): it still hits the resident lines, and an access with an
 // explicit policy sets the line's priority, so no evict_last line is left
 // behind the call.  A single pass therefore never marks lines evict_last.
+// The alternating load path (8) walks odd passes from the book's last tile
+// to its first, so each pass starts on the lines the previous pass touched
+// last, which the L2 still holds.
 inline MapCfg pass_cfg(MapCfg c, int j, int runs) {
     if (c.load_path == 7 && j == runs - 1) c.load_path = 6;
+    c.rev = (c.load_path == 8) ? (j & 1) : 0;
     return c;
 }
 // Reads and clears the bulk-staged kernel's error word (non-zero: a bounded

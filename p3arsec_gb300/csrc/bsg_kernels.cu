@@ -47,10 +47,13 @@ struct Raw {
 // first `gres` groups, a tuned fraction of the L2) with an evict_last
 // policy, the rest evict_first -- the prefix then stays in L2 from pass to
 // pass while the rest streams through.
+// LP 8: the v8 loads of LP 2 and stores with the default L2 policy, every
+// other pass in reverse tile order (the L2 keeps what it saw last).
 __host__ __device__ constexpr bool lp_resident(int lp) { return lp == 7; }
 __host__ __device__ constexpr bool lp_hinted(int lp) { return lp == 1 || lp == 6 || lp == 7; }
 __host__ __device__ constexpr bool lp_evict_first(int lp) { return lp == 1 || lp == 6; }
-__host__ __device__ constexpr bool lp_v8(int lp) { return lp == 2 || lp == 6 || lp == 7; }
+__host__ __device__ constexpr bool lp_v8(int lp) { return lp == 2 || lp == 6 || lp == 7 || lp == 8; }
+__host__ __device__ constexpr bool lp_alternating(int lp) { return lp == 8; }
 
 template <int W, int LP>
 __device__ __forceinline__ Raw<W> ld_group(const void* p, unsigned long long pol) {
@@ -87,6 +90,12 @@ __device__ __forceinline__ void st_group(float* p, const float (&x)[W], unsigned
         asm volatile("st.global.L2::cache_hint.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8}, %9;"
                      :: "l"(p), "f"(x[0]), "f"(x[1]), "f"(x[2]), "f"(x[3]),
                         "f"(x[4]), "f"(x[5]), "f"(x[6]), "f"(x[7]), "l"(pol)
+                     : "memory");
+    } else if constexpr (W == 8 && lp_alternating(LP)) {
+        (void)pol;
+        asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};"
+                     :: "l"(p), "f"(x[0]), "f"(x[1]), "f"(x[2]), "f"(x[3]),
+                        "f"(x[4]), "f"(x[5]), "f"(x[6]), "f"(x[7])
                      : "memory");
     } else if constexpr (W == 4) {
         (void)pol;
@@ -188,14 +197,17 @@ __device__ __forceinline__ void pdl_wait() {
 template <int M, int W, int VPT, int LP>
 __global__ void __launch_bounds__(M == MODE_LIBM_REF ? 256 : 512,
                                   M == MODE_LIBM_REF ? 4 : (VPT == 1 ? 2 : 1))
-    map_vec_kernel(SoA a, int64_t n, int64_t gres) {
+    map_vec_kernel(SoA a, int64_t n, int64_t gres, int rev) {
     pdl_trigger();
     const unsigned long long pol =
         (lp_evict_first(LP) || lp_resident(LP)) ? evict_first_policy() : 0ull;
     const unsigned long long pol_res = lp_resident(LP) ? evict_last_policy() : 0ull;
     const int64_t ngroups = n / W;
     const int64_t tile = (int64_t)blockDim.x * VPT;
-    for (int64_t t0 = (int64_t)blockIdx.x * tile; t0 < ngroups; t0 += (int64_t)gridDim.x * tile) {
+    const int64_t ntiles = (ngroups + tile - 1) / tile;
+    for (int64_t ti = blockIdx.x; ti < ntiles; ti += gridDim.x) {
+        // LP 8's odd passes take the tiles from the last to the first
+        const int64_t t0 = (lp_alternating(LP) && rev ? ntiles - 1 - ti : ti) * tile;
         const int64_t t1 = (t0 + tile < ngroups) ? t0 + tile : ngroups;
         price_groups<M, W, VPT, LP>(a, t0, t1, pol, pol_res, gres);
     }
@@ -521,7 +533,8 @@ static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg_in
     lc.attrs = attr;
     lc.numAttrs = cfg.pdl ? 1 : 0;
     cudaError_t le = cudaSuccess;
-#define BSG_LAUNCH(W_, V_, L_) le = cudaLaunchKernelEx(&lc, map_vec_kernel<M, W_, V_, L_>, a, n, gres)
+#define BSG_LAUNCH(W_, V_, L_) \
+    le = cudaLaunchKernelEx(&lc, map_vec_kernel<M, W_, V_, L_>, a, n, gres, cfg.rev)
     if constexpr (M == MODE_FAST) {
         switch (cfg.load_path * 10 + cfg.vpt) {
             case 1: BSG_LAUNCH(4, 1, 0); break;
@@ -536,6 +549,8 @@ static cudaError_t launch_map_mode(const SoA& a, int64_t n, const MapCfg& cfg_in
             case 62: BSG_LAUNCH(8, 2, 6); break;
             case 71: BSG_LAUNCH(8, 1, 7); break;
             case 72: BSG_LAUNCH(8, 2, 7); break;
+            case 81: BSG_LAUNCH(8, 1, 8); break;
+            case 82: BSG_LAUNCH(8, 2, 8); break;
             default: return cudaErrorInvalidValue;
         }
     } else {

@@ -160,7 +160,7 @@ def test_all_tunings_give_identical_bits(gpu_ctx):
     base = gpu_ctx.price_book(book)
     saved = gpu_ctx.get_tune()
     try:
-        for lp in (0, 1, 2, 3, 4, 5, 6, 7):
+        for lp in (0, 1, 2, 3, 4, 5, 6, 7, 8):
             for vpt in (1, 2, 4):
                 if lp >= 2 and vpt == 4:
                     continue
@@ -190,6 +190,26 @@ def test_resident_prefix_path_on_a_book_larger_than_l2(gpu_ctx):
                 got = gpu_ctx.price_book(book, num_runs=3)
                 assert np.array_equal(got.view(np.uint32), base.view(np.uint32)), \
                     (vpt, block, bps, pdl, r32)
+    finally:
+        gpu_ctx.set_tune(**saved)
+
+
+def test_alternating_path_every_pass_count(gpu_ctx):
+    """Load path 8 walks odd passes from the last tile to the first: any
+    number of passes, on a book larger than the L2 and on a ragged small
+    one, gives the bits of the plain path."""
+    saved = gpu_ctx.get_tune()
+    try:
+        for n in (4_000_003, 1001):
+            book = books.generate(n, seed=17)
+            gpu_ctx.set_tune(1, 256, 0, 0, 0)
+            base = gpu_ctx.price_book(book, num_runs=1)
+            for vpt, block, bps, pdl in ((1, 128, 4, 1), (2, 256, 0, 1), (1, 512, 2, 0)):
+                gpu_ctx.set_tune(vpt, block, bps, 8, pdl)
+                for runs in (1, 2, 3, 100):
+                    got = gpu_ctx.price_book(book, num_runs=runs)
+                    assert np.array_equal(got.view(np.uint32), base.view(np.uint32)), \
+                        (n, vpt, block, bps, pdl, runs)
     finally:
         gpu_ctx.set_tune(**saved)
 
