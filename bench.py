@@ -273,14 +273,26 @@ def run_ours(args, rank, world, local):
     l0 = ctx.launches
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    repeat_ms = []
     with ClockSampler(local) as clk:
         e0.record(stream)
         for _ in range(args.steps):
             step()
         e1.record(stream)
         e1.synchronize()
+        launches = ctx.launches - l0
+        # the same K steps timed again, to show the spread of the number
+        # (and to give the clock sampler a longer window under load)
+        for _ in range(args.repeats):
+            r0 = torch.cuda.Event(enable_timing=True)
+            r1 = torch.cuda.Event(enable_timing=True)
+            r0.record(stream)
+            for _ in range(args.steps):
+                step()
+            r1.record(stream)
+            r1.synchronize()
+            repeat_ms.append(r0.elapsed_time(r1))
     torch.cuda.synchronize()
-    launches = ctx.launches - l0
     ms = e0.elapsed_time(e1)
     barrier(dist, local)
     ms_max = reduce_max(dist, ms, local)
@@ -360,6 +372,12 @@ def run_ours(args, rank, world, local):
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
+    if repeat_ms:
+        vals = [world * n * runs * args.steps / (m / 1e3) for m in repeat_ms]
+        line["repeats"] = {"values": vals, "note": f"{len(vals)} more timed windows of the same "
+                                                   f"{args.steps} steps, right after the first",
+                           "spread": (max(vals + [value]) - min(vals + [value])) /
+                                     float(np.median(vals + [value]))}
     ctx.close()
     del dev, out
     torch.cuda.empty_cache()
@@ -1067,6 +1085,8 @@ def main(argv=None):
                     help="swaptions config: Monte Carlo paths per swaption")
     ap.add_argument("--swaption-sample", type=int, default=200_000,
                     help="swaptions config: paths per swaption of the CPU-oracle sample")
+    ap.add_argument("--repeats", type=int, default=3,
+                    help="map: extra timed windows of the same steps (their spread is reported)")
     ap.add_argument("--no-nested", action="store_true",
                     help="map: skip the nested 2^28, batch and serve records")
     ap.add_argument("--tune", default=None,

@@ -433,7 +433,7 @@ int bsg_read_soa(const char* path, bsg_book* out);
  * options and makes the fastest the context's choice: every shape over 5
  * passes; then the prefix sizes 4..24 32nds of the L2 for the best
  * resident-prefix shape over 25 passes; then the four fastest shapes over
- * 25 passes twice.  The result is cached in the file named by
+ * BSG_NUM_RUNS passes, three times each, the best time of each.  The result is cached in the file named by
  * $BSG_TUNE_CACHE (if set) per (device, size bucket). */
 typedef struct bsg_tune {
     int vec_per_thread; /* float4 groups per thread per tile: 1, 2 or 4 */

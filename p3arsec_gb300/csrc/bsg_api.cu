@@ -99,6 +99,11 @@ struct bsg_ctx {
     uint64_t* d_seg = nullptr;
     size_t seg_cap = 0;
     uint64_t* h_seg = nullptr;  // pinned staging of the same layout
+    // per-tile [begin, end) of the batch (2 entries per tile), device and
+    // pinned staging
+    uint64_t* d_tb = nullptr;
+    uint64_t* h_tb = nullptr;
+    size_t tb_cap = 0;  // tiles
     cudaEvent_t seg_ev = nullptr;
     unsigned long long* d_cursor = nullptr;  // one work counter per pass
     size_t cursor_cap = 0;
@@ -515,8 +520,26 @@ int grow_seg_scratch(bsg_ctx* c, size_t nseg) {
     return BSG_OK;
 }
 
-// Validates the segments and writes the compacted (non-empty) table into the
-// pinned staging buffer.  Returns the count of non-empty segments.
+int grow_tile_scratch(bsg_ctx* c, size_t ntiles) {
+    if (ntiles <= c->tb_cap) return BSG_OK;
+    const size_t cap = round_up(std::max<size_t>(ntiles, 4096), 4096);
+    if (c->seg_ev) BSG_CK(c, cudaEventSynchronize(c->seg_ev));
+    BSG_CK(c, cudaStreamSynchronize(c->stream));
+    graph_drop_all(c);  // graphs hold the old table address
+    if (c->d_tb) cudaFree(c->d_tb);
+    if (c->h_tb) cudaFreeHost(c->h_tb);
+    c->d_tb = nullptr;
+    c->h_tb = nullptr;
+    c->tb_cap = 0;
+    BSG_CK(c, cudaMalloc(&c->d_tb, 2 * cap * sizeof(uint64_t)));
+    BSG_CK(c, cudaMallocHost(&c->h_tb, 2 * cap * sizeof(uint64_t)));
+    c->tb_cap = cap;
+    return BSG_OK;
+}
+
+// Validates the segments and writes the compacted (non-empty) table, and
+// every tile's [begin, end), into the pinned staging buffers.  Returns the
+// count of non-empty segments.
 int build_segments(bsg_ctx* c, const bsg_segment* segs, size_t nseg, size_t pool_len,
                    uint64_t tile, int* nseg_out, uint64_t* ntiles_out) {
     std::vector<std::pair<uint64_t, uint64_t>> v;
@@ -548,6 +571,15 @@ int build_segments(bsg_ctx* c, const bsg_segment* segs, size_t nseg, size_t pool
         acc += (v[i].second + tile - 1) / tile;
     }
     pre[m] = acc;
+    if ((st = grow_tile_scratch(c, acc))) return st;
+    uint64_t* tb = c->h_tb;
+    for (size_t i = 0; i < m; ++i) {
+        const uint64_t e = off[i] + len[i];
+        for (uint64_t b = off[i]; b < e; b += tile, tb += 2) {
+            tb[0] = b;
+            tb[1] = (e - b > tile) ? b + tile : e;
+        }
+    }
     *nseg_out = (int)m;
     *ntiles_out = acc;
     return BSG_OK;
@@ -649,6 +681,8 @@ void bsg_destroy(bsg_ctx* c) {
     if (c->dev_buf) cudaFree(c->dev_buf);
     if (c->d_seg) cudaFree(c->d_seg);
     if (c->h_seg) cudaFreeHost(c->h_seg);
+    if (c->d_tb) cudaFree(c->d_tb);
+    if (c->h_tb) cudaFreeHost(c->h_tb);
     if (c->d_cursor) cudaFree(c->d_cursor);
     if (c->d_acc) cudaFree(c->d_acc);
     if (c->d_edges) cudaFree(c->d_edges);
@@ -880,6 +914,7 @@ int price_batch_impl(bsg_ctx* c, const float* s, const float* k, const float* r,
         BSG_CK(c, cudaMemcpyAsync((void*)d_off, c->h_seg, m * 8, cudaMemcpyHostToDevice, c->stream));
         BSG_CK(c, cudaMemcpyAsync((void*)d_len, c->h_seg + c->seg_cap, m * 8, cudaMemcpyHostToDevice, c->stream));
         BSG_CK(c, cudaMemcpyAsync((void*)d_pre, c->h_seg + 2 * c->seg_cap, (m + 1) * 8, cudaMemcpyHostToDevice, c->stream));
+        BSG_CK(c, cudaMemcpyAsync(c->d_tb, c->h_tb, ntiles * 16, cudaMemcpyHostToDevice, c->stream));
         BSG_CK(c, cudaEventRecord(c->seg_ev, c->stream));
         // one work counter per pass, zeroed together, so that pass j + 1 can
         // start (PDL) while pass j drains
@@ -895,8 +930,8 @@ int price_batch_impl(bsg_ctx* c, const float* s, const float* k, const float* r,
         auto all_runs = [&]() -> cudaError_t {
             cudaError_t e = cudaMemsetAsync(c->d_cursor, 0, (size_t)num_runs * 8, c->stream);
             for (int j = 0; j < num_runs && e == cudaSuccess; ++j)
-                e = bsg::launch_batch(a, d_off, d_len, d_pre, m, ntiles, topt, c->d_cursor + j,
-                                      mode, grid, j > 0 ? 1 : 0, c->stream);
+                e = bsg::launch_batch(a, d_off, d_len, d_pre, c->d_tb, m, ntiles, topt,
+                                      c->d_cursor + j, mode, grid, j > 0 ? 1 : 0, c->stream);
             return e;
         };
         if (num_runs == 1 || (flags & BSG_NO_GRAPH)) {
@@ -1434,13 +1469,14 @@ extern "C" int bsg_autotune(bsg_ctx* c, size_t n, bsg_tune* out) {
     }
     for (auto& x : timed)
         if (x.second.load_path == 7) x.second.resident_32nds = best_res;
-    // stage 3: the four fastest again over 25 passes each, twice, interleaved
-    // (longer runs show the steady state the L2 reaches across passes)
+    // stage 3: the four fastest again over NUM_RUNS passes each (a call's
+    // length: the steady state the L2 reaches across passes), three rounds
+    // interleaved, the best round of each
     if (timed.size() > 4) timed.resize(4);
     std::vector<float> fin(timed.size(), 1e30f);
-    for (int round = 0; round < 2 && e == cudaSuccess; ++round)
+    for (int round = 0; round < 3 && e == cudaSuccess; ++round)
         for (size_t q = 0; q < timed.size() && e == cudaSuccess; ++q) {
-            const float ms = time_cfg(cfg_of(timed[q].second), 25);
+            const float ms = time_cfg(cfg_of(timed[q].second), BSG_NUM_RUNS);
             if (ms >= 0 && ms < fin[q]) fin[q] = ms;
         }
     float best_ms = 1e30f;

@@ -96,14 +96,16 @@ cudaError_t launch_map_f64(const SoA64& a, int64_t n, int sm_count, cudaStream_t
 
 // Persistent batched pricing.  seg_off/seg_len/tile_prefix are device arrays
 // of nseg (tile_prefix: nseg + 1 entries, exclusive prefix of tiles of
-// tile_opts options per segment); cursor is a device counter that must be 0
-// at launch.  pdl: launch with programmatic stream serialization (the next
-// pass may start while this one drains; it must use its own cursor).
+// tile_opts options per segment); tile_bounds (optional, NULL = search the
+// prefix instead) holds each tile's [begin, end) in the pool, 2 * ntiles
+// entries; cursor is a device counter that must be 0 at launch.  pdl: launch
+// with programmatic stream serialization (the next pass may start while
+// this one drains; it must use its own cursor).
 cudaError_t launch_batch(const SoA& pool, const uint64_t* seg_off,
                          const uint64_t* seg_len, const uint64_t* tile_prefix,
-                         int nseg, uint64_t ntiles, uint64_t tile_opts,
-                         unsigned long long* cursor, int mode, int grid, int pdl,
-                         cudaStream_t st);
+                         const uint64_t* tile_bounds, int nseg, uint64_t ntiles,
+                         uint64_t tile_opts, unsigned long long* cursor, int mode, int grid,
+                         int pdl, cudaStream_t st);
 // Default options per batch tile.
 uint64_t batch_tile_options();
 // Resident blocks per SM of the batch kernel (its persistent grid = this x SMs).

@@ -646,33 +646,45 @@ __device__ __forceinline__ void price_range(const SoA& pool, uint64_t b, uint64_
 }
 
 // Persistent kernel: each block takes the next tile from the device work
-// counter, maps it to its segment by binary search over the tile prefix and
-// prices it.  No block ever waits on another; the loop ends when the counter
-// passes the last tile.  (Four blocks per SM hold the registers to 64; the
-// libm mode's float-float exp/log get up to 128.)
+// counter and prices it.  With a per-tile bounds table (tile_bounds[2 t],
+// [2 t + 1] = the tile's [b, e) in the pool) a tile costs thread 0 one load;
+// without it, a binary search over the tile prefix finds its segment.  The
+// claim of the next tile is issued before the current one is priced, so the
+// counter's round trip overlaps the pricing.  No block ever waits on another;
+// the loop ends when the counter passes the last tile.  (Four blocks per SM
+// hold the registers to 64; the libm mode's float-float exp/log get up to
+// 128.)
 template <int M, int W>
 __global__ void __launch_bounds__(kBatchBlock, M == MODE_LIBM_REF ? 2 : 4) batch_kernel(
     SoA pool, const uint64_t* __restrict__ seg_off, const uint64_t* __restrict__ seg_len,
-    const uint64_t* __restrict__ tile_prefix, int nseg, uint64_t ntiles, uint64_t topt,
-    unsigned long long* cursor) {
+    const uint64_t* __restrict__ tile_prefix, const uint64_t* __restrict__ tile_bounds, int nseg,
+    uint64_t ntiles, uint64_t topt, unsigned long long* cursor) {
     __shared__ uint64_t sh_b, sh_e;
     __shared__ int sh_done;
     pdl_trigger();
+    unsigned long long next = 0;
+    if (threadIdx.x == 0) next = atomicAdd(cursor, 1ull);
     for (;;) {
         if (threadIdx.x == 0) {
-            const unsigned long long tile = atomicAdd(cursor, 1ull);
+            const unsigned long long tile = next;
             if (tile >= ntiles) {
                 sh_done = 1;
             } else {
-                int lo = 0, hi = nseg - 1;
-                while (lo < hi) {  // largest segment whose first tile <= tile
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (tile_prefix[mid] <= tile) lo = mid; else hi = mid - 1;
+                next = atomicAdd(cursor, 1ull);  // travels while this tile is priced
+                if (tile_bounds) {
+                    sh_b = tile_bounds[2 * tile];
+                    sh_e = tile_bounds[2 * tile + 1];
+                } else {
+                    int lo = 0, hi = nseg - 1;
+                    while (lo < hi) {  // largest segment whose first tile <= tile
+                        const int mid = (lo + hi + 1) >> 1;
+                        if (tile_prefix[mid] <= tile) lo = mid; else hi = mid - 1;
+                    }
+                    const uint64_t b = seg_off[lo] + (tile - tile_prefix[lo]) * topt;
+                    const uint64_t send = seg_off[lo] + seg_len[lo];
+                    sh_b = b;
+                    sh_e = (b + topt < send) ? b + topt : send;
                 }
-                const uint64_t b = seg_off[lo] + (tile - tile_prefix[lo]) * topt;
-                const uint64_t send = seg_off[lo] + seg_len[lo];
-                sh_b = b;
-                sh_e = (b + topt < send) ? b + topt : send;
                 sh_done = 0;
             }
         }
@@ -697,9 +709,9 @@ int batch_blocks_per_sm() {
 
 cudaError_t launch_batch(const SoA& pool, const uint64_t* seg_off,
                          const uint64_t* seg_len, const uint64_t* tile_prefix,
-                         int nseg, uint64_t ntiles, uint64_t tile_opts,
-                         unsigned long long* cursor, int mode, int grid, int pdl,
-                         cudaStream_t st) {
+                         const uint64_t* tile_bounds, int nseg, uint64_t ntiles,
+                         uint64_t tile_opts, unsigned long long* cursor, int mode, int grid,
+                         int pdl, cudaStream_t st) {
     if (ntiles == 0 || nseg <= 0) return cudaSuccess;
     if (tile_opts == 0) return cudaErrorInvalidValue;
     if ((uint64_t)grid > ntiles) grid = (int)ntiles;  // no block without a tile
@@ -717,10 +729,10 @@ cudaError_t launch_batch(const SoA& pool, const uint64_t* seg_off,
     // keeps 128-bit loads (fewer registers: it is compute-bound)
     const bool w8 = mode != MODE_LIBM_REF && map_vectorizable(pool, MapCfg{1, kBatchBlock, 0, 2, 0});
 #define BSG_BATCH(M_) \
-    (w8 ? cudaLaunchKernelEx(&lc, batch_kernel<M_, 8>, pool, seg_off, seg_len, tile_prefix, nseg, \
-                             ntiles, tile_opts, cursor) \
-        : cudaLaunchKernelEx(&lc, batch_kernel<M_, 4>, pool, seg_off, seg_len, tile_prefix, nseg, \
-                             ntiles, tile_opts, cursor))
+    (w8 ? cudaLaunchKernelEx(&lc, batch_kernel<M_, 8>, pool, seg_off, seg_len, tile_prefix, \
+                             tile_bounds, nseg, ntiles, tile_opts, cursor) \
+        : cudaLaunchKernelEx(&lc, batch_kernel<M_, 4>, pool, seg_off, seg_len, tile_prefix, \
+                             tile_bounds, nseg, ntiles, tile_opts, cursor))
     switch (mode) {
         case MODE_FAST: return BSG_BATCH(MODE_FAST);
         case MODE_SFU_REF: return BSG_BATCH(MODE_SFU_REF);

@@ -671,7 +671,7 @@ struct bsg_server {
         if (cudaGetLastError() != cudaSuccess) return BSG_ERR_CUDA;
         if (cudaMemsetAsync(sl.d_cursor, 0, sizeof(unsigned long long), sl.st) != cudaSuccess)
             return BSG_ERR_CUDA;
-        if (bsg::launch_batch(pool, doff, dlen, dpre, m, ntiles, kTile, sl.d_cursor, mode,
+        if (bsg::launch_batch(pool, doff, dlen, dpre, nullptr, m, ntiles, kTile, sl.d_cursor, mode,
                               batch_grid, 0, sl.st) != cudaSuccess)
             return BSG_ERR_CUDA;
         egress_kernel<<<grid, kThreads, 0, sl.st>>>(dd, dpre, m, ntiles, pool.out);
