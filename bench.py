@@ -6,16 +6,18 @@ Default workload (the headline): the plain map over 10,000,000 seeded options
 calls/puts 50/50), FP32, NUM_RUNS = 100 passes per step -- one step is one
 whole ROI of the reference benchmark (blackscholes.c:781-913).  The 280 MB
 working set is larger than the 129 MB L2, but only 2.2x: cross-pass L2 hits
-serve part of it (the line says so), so the same line carries three nested
+serve part of it (the line says so), so the same line carries four nested
 records measured in the same run:
 
-* ``roofline_2p28`` -- the map over 2^28 options (7.5 GB, 58x the L2): the
+* ``roofline_2p28`` -- the map over 2^28 options (7.5 GB, 55x the L2): the
   HBM-roofline fraction with nothing L2-resident;
 * ``batch`` -- 4,096 books of log-uniform size in one persistent CUDA-graph
   launch per pass vs one plain launch per book per pass;
 * ``serve`` -- an open-loop Poisson trace through the continuous-batching
   server vs one plain launch per request, with the throughput each sustains
-  under p99 bounds of 0.5, 1 and 2 ms (medians of repeated traces).
+  under p99 bounds of 0.5, 1 and 2 ms (medians of repeated traces);
+* ``swaptions`` -- the swaptions application's HJM Monte Carlo, 128
+  swaptions x 1,000,000 paths in one call, with the CPU oracle on a sample.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--config map|batch|precision|serve|io|fp64|prefix-sweep|swaptions]
@@ -385,6 +387,8 @@ def run_ours(args, rank, world, local):
         line["roofline_2p28"] = _nested(map_2p28_record, args, local, peak, peak_src)
         line["batch"] = _nested(batch_record, args, local, steps=3, warmup=3)
         line["serve"] = _nested(serve_record, args, local)
+        line["swaptions"] = _nested(swaptions_record, args, local, steps=3, warmup=3,
+                                    sample=20_000)
         torch.cuda.empty_cache()
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(book)
@@ -889,68 +893,82 @@ def run_io(args, rank, world, local):
 
 
 # --------------------------------------------------------------- swaptions
-def run_swaptions(args, rank, world, local):
+def swaptions_record(args, local, nsw=None, trials=None, steps=None, warmup=None, sample=None):
     """The swaptions application (P3ARSEC's HJM Monte Carlo,
-    HJM_Swaption_Blocking.cpp): args.swaptions swaptions of the reference
-    driver's kind, args.trials paths each, priced in one call of
-    bsg_price_swaptions; the CPU oracle (the same model and random stream,
-    the whole path matrix as the reference simulates it) on every host core
-    over a bounded sample is the CPU baseline, and the GPU's prices on that
-    sample are checked against it."""
-    import torch
-
+    HJM_Swaption_Blocking.cpp): nsw swaptions of the reference driver's
+    kind, `trials` paths each, priced in one call of bsg_price_swaptions per
+    step (host arrays in, prices out, the call synchronises); the CPU oracle
+    (the same model and random stream, the whole path matrix as the
+    reference simulates it) on every host core over `sample` paths per
+    swaption is the CPU baseline, and the GPU's prices on that sample are
+    checked against it."""
     import oracle
     from p3arsec_gb300 import Context
-    from p3arsec_gb300 import build as b
     from p3arsec_gb300 import swaptions as S
-    b.build()
     oracle.build(ref=False)
-    torch.cuda.set_device(local)
-    sw = S.generate(args.swaptions, seed=1979)
+    nsw = args.swaptions if nsw is None else nsw
+    trials = args.trials if trials is None else trials
+    steps = args.steps if steps is None else steps
+    warmup = args.warmup if warmup is None else warmup
+    sample = min(trials, args.swaption_sample if sample is None else sample)
+    sw = S.generate(nsw, seed=1979)
     ctx = Context(local, max_options=1)
-    trials = args.trials
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         ctx.price_swaptions(sw, trials)
     l0 = ctx.launches
     times = []
     with ClockSampler(local) as clk:
-        for _ in range(args.steps):
+        for _ in range(steps):
             t0 = time.perf_counter()
             price, err = ctx.price_swaptions(sw, trials)
             times.append(time.perf_counter() - t0)
     launches = ctx.launches - l0
     secs = float(np.median(times))
-    paths = len(sw) * trials
-    # the same swaptions on a sample of the trials, GPU and CPU oracle
-    sample = min(trials, args.swaption_sample)
-    g_s, g_e = ctx.price_swaptions(sw, sample)
+    g_s, _ = ctx.price_swaptions(sw, sample)
+    ctx.close()
     threads = os.cpu_count() or 1
-    c_s, c_e, c_secs = oracle.swaptions_all(sw, sample, threads)
+    c_s, _, c_secs = oracle.swaptions_all(sw, sample, threads)
     rel = float(np.max(np.abs(g_s - c_s) / np.maximum(np.abs(c_s), 1e-12)))
-    line = {
-        "metric": "swaption paths/s (HJM Monte Carlo, FP64)",
-        "value": paths / secs, "unit": "paths/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * secs, "higher_is_better": True,
-        "dtype": "f64", "data": "synthetic (the reference driver's swaption set, seeded)",
-        "config": {"workload": f"{len(sw)} swaptions x {trials} paths, 11-point HJM grid, "
-                               "3 factors, one bsg_price_swaptions call per step (host arrays in, "
-                               "prices out)", "swaptions": len(sw), "trials": trials},
+    return {
+        "workload": f"{nsw} swaptions x {trials} paths, 11-point HJM grid, 3 factors, one "
+                    "bsg_price_swaptions call per step (host arrays in, prices out)",
+        "swaptions": nsw, "trials": trials, "steps": steps, "warmup": warmup,
+        "value": nsw * trials / secs, "unit": "paths/s", "ms_per_step": 1e3 * secs,
+        "dtype": "f64",
         "step_time_s": {"median": secs, "min": min(times), "max": max(times)},
         "prices": {"first": price[:4].tolist(), "std_err_first": err[:4].tolist()},
         "gpu_launches": launches,
+        "bound": "fp64 issue (the kernel reads no bulk data; ncu: FP64 pipe at ~87 % of peak)",
         "vs_oracle": {"sample_trials": sample, "max_rel_price_diff": rel,
                       "note": "the same paths on the CPU oracle; parity with the reference "
                               "itself is unpinned (its model core is not in its tree)"},
-        "cpu_baseline": {"value": len(sw) * sample / c_secs, "unit": "paths/s",
-                         "cores": threads, "kind": "port",
-                         "sample": f"{len(sw)} swaptions x {sample} paths, static partition over "
+        "cpu_baseline": {"value": nsw * sample / c_secs, "unit": "paths/s", "cores": threads,
+                         "kind": "port",
+                         "sample": f"{nsw} swaptions x {sample} paths, static partition over "
                                    f"{threads} threads, {c_secs:.2f} s (the oracle simulates every "
                                    "row of each path, as the reference does)"},
         "clocks": clk.summary(),
     }
+
+
+def run_swaptions(args, rank, world, local):
+    """--config swaptions: the swaptions record as its own JSON line."""
+    import torch
+
+    from p3arsec_gb300 import build as b
+    b.build()
+    torch.cuda.set_device(local)
+    rec = swaptions_record(args, local)
+    line = {"metric": "swaption paths/s (HJM Monte Carlo, FP64)", "value": rec["value"],
+            "unit": "paths/s", "n_gpus": world, "steps": rec["steps"], "warmup": rec["warmup"],
+            "ms_per_step": rec["ms_per_step"], "higher_is_better": True, "dtype": "f64",
+            "data": "synthetic (the reference driver's swaption set, seeded)",
+            "config": {"workload": rec["workload"], "swaptions": rec["swaptions"],
+                       "trials": rec["trials"]},
+            **{k: rec[k] for k in ("step_time_s", "prices", "gpu_launches", "bound", "vs_oracle",
+                                   "cpu_baseline", "clocks")}}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
 
 
 # ---------------------------------------------------- resident-prefix sweep
