@@ -43,11 +43,14 @@ void swo_philox4x32_10(const uint32_t c[4], const uint32_t k[2], uint32_t out[4]
     out[3] = x3;
 }
 
-/* (0, 1) with 53 random bits: (k + 1/2) / 2^53, k from the top 27 bits of a
- * and the top 26 bits of b. */
-static double unit53(uint32_t a, uint32_t b) {
-    const double k = (double)(a >> 5) * 67108864.0 + (double)(b >> 6);
-    return (k + 0.5) * (1.0 / 9007199254740992.0);
+/* (0, 1) from 52 random bits k (the top 20 bits of a, all of b): the double
+ * 1 + k 2^-52 built from its bits, minus 1 (exact), plus 2^-53 (exact):
+ * (2k + 1) 2^-53. */
+static double unit52(uint32_t a, uint32_t b) {
+    const uint64_t bits = 0x3FF0000000000000ull | ((uint64_t)(a >> 12) << 32) | b;
+    double d;
+    memcpy(&d, &bits, sizeof d);
+    return (d - 1.0) + 1.1102230246251565e-16;
 }
 
 void swo_normal_pair(uint64_t seed, uint64_t trial, uint32_t j, double z[2]) {
@@ -55,7 +58,7 @@ void swo_normal_pair(uint64_t seed, uint64_t trial, uint32_t j, double z[2]) {
     const uint32_t k[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
     uint32_t x[4];
     swo_philox4x32_10(c, k, x);
-    const double u1 = unit53(x[0], x[1]), u2 = unit53(x[2], x[3]);
+    const double u1 = unit52(x[0], x[1]), u2 = unit52(x[2], x[3]);
     const double r = sqrt(-2.0 * log(u1));
     const double th = 6.283185307179586 * u2;
     z[0] = r * cos(th);

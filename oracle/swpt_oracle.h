@@ -56,7 +56,7 @@ typedef struct swo_swaption {
 /* Philox4x32-10 of counter c[4] under key k[2] into out[4]. */
 void swo_philox4x32_10(const uint32_t c[4], const uint32_t k[2], uint32_t out[4]);
 
-/* Normal variates 2j and 2j + 1 of one trial: Box-Muller of the two 53-bit
+/* Normal variates 2j and 2j + 1 of one trial: Box-Muller of the two 52-bit
  * uniforms that Philox draws for counter (trial, j). */
 void swo_normal_pair(uint64_t seed, uint64_t trial, uint32_t j, double z[2]);
 

@@ -59,27 +59,30 @@ __device__ __forceinline__ void philox4x32_10(uint32_t x0, uint32_t x1, uint32_t
     out[3] = x3;
 }
 
-// (0, 1) from 53 random bits: (k + 1/2) / 2^53.
-__device__ __forceinline__ double unit53(uint32_t a, uint32_t b) {
-    const double k = __fma_rn((double)(a >> 5), 67108864.0, (double)(b >> 6));
-    return (k + 0.5) * (1.0 / 9007199254740992.0);
+// (0, 1) from 52 random bits k (the top 20 bits of a, all of b): the double
+// 1 + k 2^-52 built from its bits, minus 1, plus 2^-53 -- (2k + 1) 2^-53,
+// both additions exact, two double operations and no conversion.
+__device__ __forceinline__ double unit52(uint32_t a, uint32_t b) {
+    const double d = __hiloint2double((int)(0x3FF00000u | (a >> 12)), (int)b);
+    return __dadd_rn(__dadd_rn(d, -1.0), 1.1102230246251565e-16);
 }
 
-// Normal variates 2j and 2j + 1 of trial t.
+// Normal variates 2j and 2j + 1 of trial t: Box-Muller, the angle 2 pi u2
+// evaluated as sincospi(2 u2) (2 u2 is exact; no reduction by pi needed).
 __device__ __forceinline__ void normal_pair(uint64_t seed, uint64_t t, uint32_t j, double& z0,
                                             double& z1) {
     uint32_t x[4];
     philox4x32_10((uint32_t)t, (uint32_t)(t >> 32), j, 0u, (uint32_t)seed, (uint32_t)(seed >> 32), x);
-    const double u1 = unit53(x[0], x[1]), u2 = unit53(x[2], x[3]);
+    const double u1 = unit52(x[0], x[1]), u2 = unit52(x[2], x[3]);
     const double r = sqrt(-2.0 * log(u1));
     double s, c;
-    sincos(6.283185307179586 * u2, &s, &c);
+    sincospi(2.0 * u2, &s, &c);
     z0 = r * c;
     z1 = r * s;
 }
 
 // Per-swaption constants in shared memory: the forward curve, the drift
-// times h, the vols, the swap payments.
+// times h, the vols times sqrt(h), the swap payments.
 template <int MAXN>
 struct SwShared {
     double fwd[MAXN];
@@ -115,13 +118,12 @@ __global__ void __launch_bounds__(kSwThreads, 2) swaption_paths_kernel(const SwP
             for (int m = 0; m < i && m < n - 1; ++m) s_prev += p.vol[k][m];
             const double vk = i < n - 1 ? p.vol[k][i] : 0.0;
             mu += h * vk * (s_prev + 0.5 * vk);
-            sh.vol[k][i] = vk;
+            sh.vol[k][i] = vk * p.sqh;
         }
         sh.muh[i] = mu * h;
     }
     __syncthreads();
     const int s = p.start, L = p.swap_len;
-    const double sqh = p.sqh;
     const uint64_t base = (uint64_t)blockIdx.x * per_thread * kSwThreads;
     double sum = 0.0, sum_sq = 0.0;
     for (int q = 0; q < per_thread; ++q) {
@@ -145,7 +147,7 @@ __global__ void __launch_bounds__(kSwThreads, 2) swaption_paths_kernel(const SwP
             }
             // row i + 1 from row i (entries past n - 1 - i are never read)
 #pragma unroll
-            for (int m = 0; m < MAXN - 1; ++m) f[m] = f[m + 1] + sh.muh[m] + sqh * shock[m];
+            for (int m = 0; m < MAXN - 1; ++m) f[m] = f[m + 1] + sh.muh[m] + shock[m];
         }
         const double disc = exp(-acc * h);
         double fixed = 0.0, accs = 0.0;
