@@ -1,7 +1,8 @@
-"""In-tree build of libbsgpu.so (sm_103a) and the drop-in blackscholes CLI.
+"""In-tree build of libbsgpu.so (sm_103a) and the drop-in blackscholes and
+swaptions CLIs.
 
 Compiles each translation unit with nvcc in parallel, links the shared
-library next to this file and the CLI into ``p3arsec_gb300/bin/``.  No
+library next to this file and the CLIs into ``p3arsec_gb300/bin/``.  No
 torch, no cmake: ``python -m p3arsec_gb300.build`` or ``build()``.
 """
 from __future__ import annotations
@@ -19,6 +20,7 @@ HOST = os.path.join(PKG, "host")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libbsgpu.so")
 CLI = os.path.join(PKG, "bin", "blackscholes_gpu")
+SWAPTIONS_CLI = os.path.join(PKG, "bin", "swaptions_gpu")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -103,14 +105,15 @@ def _build_locked(verbose: bool, force: bool) -> str:
         tmp = LIB + ".tmp"
         _run([nv] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"])
         os.replace(tmp, LIB)
-    cli_src = os.path.join(HOST, "blackscholes_gpu.cpp")
-    if os.path.exists(cli_src) and (force or _stale(CLI, [cli_src, LIB] + heads)):
-        os.makedirs(os.path.dirname(CLI), exist_ok=True)
-        tmp = CLI + ".tmp"
-        _run(["g++", "-O2", "-std=c++17", "-Wall", "-I" + os.path.join(ROOT, "include"),
-              cli_src, "-o", tmp, "-L" + PKG, "-lbsgpu", "-Wl,-rpath,$ORIGIN/..",
-              "-lpthread"])
-        os.replace(tmp, CLI)
+    for exe, src in ((CLI, "blackscholes_gpu.cpp"), (SWAPTIONS_CLI, "swaptions_gpu.cpp")):
+        cli_src = os.path.join(HOST, src)
+        if os.path.exists(cli_src) and (force or _stale(exe, [cli_src, LIB] + heads)):
+            os.makedirs(os.path.dirname(exe), exist_ok=True)
+            tmp = exe + ".tmp"
+            _run(["g++", "-O2", "-std=c++17", "-Wall", "-I" + os.path.join(ROOT, "include"),
+                  cli_src, "-o", tmp, "-L" + PKG, "-lbsgpu", "-Wl,-rpath,$ORIGIN/..",
+                  "-lpthread"])
+            os.replace(tmp, exe)
     return LIB
 
 

@@ -29,6 +29,16 @@ FACTORS = np.array([
 ], dtype=np.float64)
 
 
+def reference_yields(n: int = N_STEPS) -> np.ndarray:
+    """The yield curve as the reference builds it: 0.1, then each point the
+    previous one plus 0.005 (HJM_Securities.cpp:288-290)."""
+    y = np.empty(n, dtype=np.float64)
+    y[0] = .1
+    for j in range(1, n):
+        y[j] = y[j - 1] + .005
+    return y
+
+
 @dataclasses.dataclass
 class Swaption:
     """One swaption: the reference's parm fields (HJM_Securities.cpp:276-296)."""
@@ -39,8 +49,7 @@ class Swaption:
     maturity: float = 1.0
     tenor: float = 2.0
     payment_interval: float = 1.0
-    yield_curve: np.ndarray = dataclasses.field(
-        default_factory=lambda: 0.1 + 0.005 * np.arange(N_STEPS, dtype=np.float64))
+    yield_curve: np.ndarray = dataclasses.field(default_factory=lambda: reference_yields())
     factors: np.ndarray = dataclasses.field(default_factory=lambda: FACTORS.copy())
     seed: int = 0
 
@@ -51,6 +60,35 @@ class Swaption:
     @property
     def n_factors(self) -> int:
         return int(self.factors.shape[0])
+
+
+class SplitMix64:
+    """The CLI's parameter stream (host/swaptions_gpu.cpp): splitmix64,
+    u = top 53 bits / 2^53."""
+
+    def __init__(self, seed: int):
+        self.s = seed & (2**64 - 1)
+
+    def unit(self) -> float:
+        m = 2**64 - 1
+        self.s = (self.s + 0x9E3779B97F4A7C15) & m
+        z = self.s
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & m
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & m
+        z ^= z >> 31
+        return (z >> 11) * (1.0 / 9007199254740992.0)
+
+
+def generate_cli(n: int, seed: int = 1979) -> list[Swaption]:
+    """The swaption set the drop-in CLI builds for `-ns n -sd seed`."""
+    rng = SplitMix64(seed)
+    base = int(2147483647 * rng.unit())
+    out = []
+    for i in range(n):
+        years = 5.0 + int(60 * rng.unit()) * 0.25
+        strike = 0.1 + int(49 * rng.unit()) * 0.1
+        out.append(Swaption(strike=strike, years=years, seed=base + i))
+    return out
 
 
 def generate(n: int, seed: int = 1979) -> list[Swaption]:

@@ -36,3 +36,29 @@ def test_cli_bad_input_exits_1(tmp_path):
     r = subprocess.run([build.CLI, "1", str(bad), str(tmp_path / "o.txt")],
                        stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=60)
     assert r.returncode == 1 and "ERROR" in r.stdout
+
+
+# ------------------------------------------------------------ swaptions CLI
+def _swaptions_cli(*args, timeout=120):
+    build.build()
+    return subprocess.run([build.SWAPTIONS_CLI, *args], stdout=subprocess.PIPE,
+                          stderr=subprocess.PIPE, text=True, timeout=timeout)
+
+
+def test_swaptions_cli_prices_like_the_oracle():
+    """The swaptions drop-in (HJM_Securities.cpp's main): reference options and
+    output lines; every printed price and standard error equals the CPU
+    oracle's on the same swaption set and paths (to the 10 decimals printed
+    and the oracle's tolerance)."""
+    from p3arsec_gb300 import swaptions as S
+    r = _swaptions_cli("-ns", "6", "-sm", "20000", "-nt", "2", "-sd", "7")
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Number of Simulations: 20000,  Number of threads: 2 Number of swaptions: 6" in r.stdout
+    assert "roi.time|" in r.stdout
+    lines = [l for l in r.stderr.splitlines() if l.startswith("Swaption ")]
+    assert len(lines) == 6
+    got = np.array([[float(x) for x in l.split("SwaptionPrice: ")[1].split(" StdError: ")[0:1]]
+                    + [float(l.split("StdError: ")[1].rstrip("] "))] for l in lines])
+    want, want_err, _ = oracle.swaptions_all(S.generate_cli(6, seed=7), 20000, 4)
+    assert np.allclose(got[:, 0], want, rtol=1e-10, atol=1e-9)
+    assert np.allclose(got[:, 1], want_err, rtol=1e-6, atol=1e-9)
