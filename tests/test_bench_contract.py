@@ -54,3 +54,28 @@ def test_reference_arm_under_torchrun_two_ranks():
     lines = json_lines(r.stdout)
     assert len(lines) == 1  # rank 0 only
     check_line(lines[0])
+
+
+def test_both_arms_print_the_same_config():
+    """The reference arm's config is the map's own config dict (no keys that
+    only the GPU arm knows), so a comparison of the two lines' configs holds."""
+    import bench
+    r = subprocess.run([sys.executable, "bench.py"] + ARGS, cwd=ROOT, stdout=subprocess.PIPE,
+                       stderr=subprocess.PIPE, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json_lines(r.stdout)[0]
+    assert line["config"] == bench.map_config(50000, 2, 1)
+    assert line["cpu_baseline"]["note"]
+
+
+def test_prefix_bytes_follows_the_library_rule():
+    import bench
+    l2 = 135528448.0
+    tune = {"load_path": 7, "resident_32nds": 10}
+    # 10/32 of the L2 in whole 8-option groups of 28 bytes
+    assert bench.prefix_bytes(tune, 10_000_000, l2) == (int(l2) * 10 // 32 // 224) * 224
+    assert bench.prefix_bytes({"load_path": 7, "resident_32nds": 0}, 10_000_000, l2) == \
+        (int(l2) * 15 // 32 // 224) * 224
+    assert bench.prefix_bytes({"load_path": 2}, 10_000_000, l2) == 0
+    assert bench.prefix_bytes(tune, 1000, l2) == 1000 // 8 * 8 * 28  # the whole (small) book
+
