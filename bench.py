@@ -653,9 +653,9 @@ def serve_host_pool(local, pool_n=1 << 24):
     return host, out
 
 
-def serve_point(host, out, mode, rate, seconds, args, local, seed):
+def serve_point(host, out, mode, rate, seconds, args, local, seed, sizes=None):
     from p3arsec_gb300 import abi
-    lo_n, hi_n = (int(x) for x in args.serve_sizes.split(","))
+    lo_n, hi_n = sizes or (int(x) for x in args.serve_sizes.split(","))
     return abi.serve_trace(host, out, rate_per_s=rate, duration_s=seconds, min_n=lo_n,
                            max_n=hi_n, seed=seed, device=local, budget_bytes=64 << 30,
                            max_inflight=args.serve_inflight, plain=(mode == "plain"),
@@ -710,6 +710,14 @@ def serve_record(args, local, repeats=3, trace_rate=20000.0, trace_seconds=5.0,
 
     link = host_link_bandwidth(local)
     link_opts = link["h2d_GBps"] * 1e9 / 24
+    # one request's own time: 2^20-option requests, one at a time (500/s),
+    # against the time its 24 MB in and 4 MB out take on the link alone
+    big = 1 << 20
+    alone = {m: serve_point(host, out, m, 500.0, 2.0, args, local, SEED + 99, sizes=(big, big))
+             for m in ("batched", "plain")}
+    single = {m: {"p50_ms": 1e3 * r["p50_s"], "p99_ms": 1e3 * r["p99_s"]} for m, r in alone.items()}
+    single["link_alone_ms"] = 1e3 * (24 * big / (link["h2d_GBps"] * 1e9) +
+                                     4 * big / (link["d2h_GBps"] * 1e9))
     equal = []
     for bound in SERVE_BOUNDS_MS:
         bb, pp = best("batched", bound), best("plain", bound)
@@ -733,6 +741,7 @@ def serve_record(args, local, repeats=3, trace_rate=20000.0, trace_seconds=5.0,
                       "one D2H copy, event polled",
         "trace": trace,
         "throughput_at_equal_p99": equal,
+        "single_request_2p20": single,
         "host_link": link,
         "roofline": {"bound": "host link (H2D)", "achieved": sat * 24 / 1e9,
                      "peak": link["h2d_GBps"], "unit": "GB/s",
@@ -763,8 +772,8 @@ def run_serve(args, rank, world, local):
             "dtype": "f32", "data": "synthetic (seeded trace and books)",
             "config": {"workload": rec["workload"], "batched_path": rec["batched_path"],
                        "plain_path": rec["plain_path"]},
-            **{k: rec[k] for k in ("trace", "throughput_at_equal_p99", "host_link", "roofline",
-                                   "sweep")}}
+            **{k: rec[k] for k in ("trace", "throughput_at_equal_p99", "single_request_2p20",
+                                   "host_link", "roofline", "sweep")}}
     if rank == 0:
         print(json.dumps(line), flush=True)
 
