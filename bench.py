@@ -6,7 +6,7 @@ Default workload (the headline): the plain map over 10,000,000 seeded options
 calls/puts 50/50), FP32, NUM_RUNS = 100 passes per step -- one step is one
 whole ROI of the reference benchmark (blackscholes.c:781-913).  The 280 MB
 working set is larger than the 129 MB L2, but only 2.2x: cross-pass L2 hits
-serve part of it (the line says so), so the same line carries four nested
+serve part of it (the line says so), so the same line carries nested
 records measured in the same run:
 
 * ``roofline_2p28`` -- the map over 2^28 options (7.5 GB, 55x the L2): the
@@ -17,7 +17,12 @@ records measured in the same run:
   server vs one plain launch per request, with the throughput each sustains
   under p99 bounds of 0.5, 1 and 2 ms (medians of repeated traces);
 * ``swaptions`` -- the swaptions application's HJM Monte Carlo, 128
-  swaptions x 1,000,000 paths in one call, with the CPU oracle on a sample.
+  swaptions x 1,000,000 paths in one call, with the CPU oracle on a sample;
+* ``precision`` -- 2^28 options with deep in/out-of-the-money tails, each
+  arithmetic mode's error against the FP64 kernel per |d1| bucket;
+* ``fp64`` -- the FP64 product mode (double storage) against the CPU FP64
+  oracle; ``io`` -- the reference's file formats, parsed and written, against
+  the reference's fscanf / fprintf loops.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--config map|batch|precision|serve|io|fp64|prefix-sweep|swaptions]
@@ -389,6 +394,10 @@ def run_ours(args, rank, world, local):
         line["serve"] = _nested(serve_record, args, local)
         line["swaptions"] = _nested(swaptions_record, args, local, steps=3, warmup=3,
                                     sample=20_000)
+        line["precision"] = _nested(precision_record, args, local, n=N_2P28, runs=10, steps=1,
+                                    warmup=3)
+        line["fp64"] = _nested(fp64_record, args, local, n=1 << 22, runs=10, steps=3, warmup=3)
+        line["io"] = _nested(io_record, args, n=1 << 20)
         torch.cuda.empty_cache()
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(book)
@@ -556,21 +565,20 @@ def run_batch(args, rank, world, local):
 
 
 # --------------------------------------------------------- precision sweep
-def run_precision(args, rank, world, local):
-    """Config 3: 2^28 options with deep in/out-of-the-money tails; the
-    compensated FP32 path, the reference-order SFU path and the
-    reference-order accurate-libm path against the FP64 oracle kernel, per
-    bucket of |d1|, with the throughput of each."""
+def precision_record(args, local, n=None, runs=None, steps=None, warmup=None):
+    """Config 3: options with deep in/out-of-the-money tails (K = S*U[0.05,20],
+    t ~ U[0.001,5], drawn on the GPU); the compensated FP32 path, the
+    reference-order SFU path and the reference-order accurate-libm path
+    against the FP64 oracle kernel, per bucket of |d1|, with the throughput
+    of each."""
     import torch
 
     from p3arsec_gb300 import Context, books
-    from p3arsec_gb300 import build as b
-    b.build()
-    torch.cuda.set_device(local)
-    n = args.n
-    book = books.generate(n, seed=SEED + 3, dist="tails")
-    dev = [torch.from_numpy(a).to(f"cuda:{local}") for a in book.arrays()]
-    del book
+    n = args.n if n is None else n
+    runs = args.runs if runs is None else runs
+    steps = args.steps if steps is None else steps
+    warmup = args.warmup if warmup is None else warmup
+    dev = books.generate_device(n, SEED + 3, dist="tails", device=f"cuda:{local}")
     out = torch.empty(n, dtype=torch.float32, device=f"cuda:{local}")
     ctx = Context(local, max_options=1)
     if args.tune:
@@ -582,36 +590,46 @@ def run_precision(args, rank, world, local):
     res = {}
     for mode in ("fast", "sfu_ref", "libm_ref"):
         def step():
-            ctx.price_soa(*dev, out, n=n, num_runs=args.runs, mode=mode, device=True,
+            ctx.price_soa(*dev, out, n=n, num_runs=runs, mode=mode, device=True,
                           asynchronous=True)
-        for _ in range(args.warmup):
-            step()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
-            step()
-        e1.record(stream)
-        e1.synchronize()
-        secs = e0.elapsed_time(e1) / 1e3
+        secs, _ = time_steps(stream, step, steps, warmup)
         rep = ctx.error_report(dev, out, n, edges, rel_floor=1e-3)
-        res[mode] = {"options_per_s": n * args.runs * args.steps / secs,
+        res[mode] = {"options_per_s": n * runs * steps / secs,
                      "max_abs": max(x["max_abs"] for x in rep),
                      "rms_abs": (sum(x["sum_sq_abs"] for x in rep) / n) ** 0.5,
                      "buckets": [{"d1": [x["d1_lo"], x["d1_hi"]], "count": x["count"],
                                   "max_abs": x["max_abs"], "rms_abs": x["rms_abs"],
                                   "max_rel": x["max_rel"], "max_price": x["max_price"]}
                                  for x in rep]}
+    ctx.close()
+    del dev, out
+    torch.cuda.empty_cache()
+    return {"workload": f"precision sweep, {n} options, tails distribution (K=S*U[0.05,20], "
+                        f"t~U[0.001,5], drawn on the GPU), {runs} passes per step",
+            "options": n, "num_runs": runs, "steps": steps, "warmup": warmup,
+            "rel_floor": 1e-3, "modes": res,
+            "note": "prices reach ~3.8e3 here, where one FP32 ulp is 2.4e-4: no FP32 output "
+                    "meets 1e-4 absolute in the top buckets; the 1e-4 gate is the plain "
+                    "distribution's (the headline's accuracy record)"}
+
+
+def run_precision(args, rank, world, local):
+    """--config precision: the precision record as its own JSON line."""
+    import torch
+
+    from p3arsec_gb300 import build as b
+    b.build()
+    torch.cuda.set_device(local)
+    rec = precision_record(args, local)
     line = {"metric": "precision sweep: max/RMS error vs FP64 per |d1| bucket",
-            "value": res["fast"]["options_per_s"], "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "value": rec["modes"]["fast"]["options_per_s"], "unit": UNIT, "n_gpus": world,
+            "steps": rec["steps"], "warmup": rec["warmup"], "higher_is_better": True,
             "dtype": "f32", "data": "synthetic (seeded, K=S*U[0.05,20], t~U[0.001,5])",
-            "config": {"workload": f"precision sweep, {n} options, tails distribution",
-                       "options": n, "num_runs": args.runs, "rel_floor": 1e-3},
-            "modes": res}
+            "config": {"workload": rec["workload"], "options": rec["options"],
+                       "num_runs": rec["num_runs"], "rel_floor": 1e-3},
+            "modes": rec["modes"]}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
 
 
 # ----------------------------------------------------------------- serving
@@ -779,17 +797,19 @@ def run_serve(args, rank, world, local):
 
 
 # --------------------------------------------------------- FP64 product mode
-def run_fp64(args, rank, world, local):
+def fp64_record(args, local, n=None, runs=None, steps=None, warmup=None):
     """The FP64 product mode (double storage, the SIMD variant's NCO = 2
-    types): options/s of num_runs passes, and the roofline that binds it."""
+    types): options/s of num_runs passes, the roofline that binds it, and
+    its prices against the CPU FP64 oracle (timed single-threaded as the
+    baseline of this mode)."""
     import torch
 
     import oracle
     from p3arsec_gb300 import Context, books
-    from p3arsec_gb300 import build as b
-    b.build()
-    torch.cuda.set_device(local)
-    n, runs = args.n, args.runs
+    n = args.n if n is None else n
+    runs = args.runs if runs is None else runs
+    steps = args.steps if steps is None else steps
+    warmup = args.warmup if warmup is None else warmup
     book = books.generate(n, seed=SEED + 8)
     dev = [torch.from_numpy(a).to(f"cuda:{local}") for a in oracle.widened(book)]
     ot = torch.from_numpy(book.otype).to(f"cuda:{local}")
@@ -800,42 +820,56 @@ def run_fp64(args, rank, world, local):
     def step():
         ctx.price_soa_f64(*dev, ot, out, n=n, num_runs=runs, device=True, asynchronous=True)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
     l0 = ctx.launches
-    with ClockSampler(local) as clk:
-        e0.record(stream)
-        for _ in range(args.steps):
-            step()
-        e1.record(stream)
-        e1.synchronize()
-    secs = e0.elapsed_time(e1) / 1e3
-    sample = np.random.default_rng(1).choice(n, min(n, 200000), replace=False)
-    got = out.cpu().numpy()[sample]
-    want = oracle.price_fp64(book.slice(0, n))[sample] if n <= (1 << 22) else None
-    value = n * runs * args.steps / secs
-    line = {"metric": "FP64 product mode: options/s (double storage)", "value": value, "unit": UNIT,
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True, "dtype": "f64",
-            "data": "synthetic (seeded book widened to double)",
-            "config": {"workload": f"FP64 map, {n} options, {runs} passes per step",
-                       "options": n, "num_runs": runs},
+    secs, clk = time_steps(stream, step, steps, 0, clocks_device=local)
+    launches = ctx.launches - l0
+    got = out.cpu().numpy()
+    ctx.close()
+    cpu = None
+    rel = None
+    if n <= (1 << 22):
+        t0 = time.perf_counter()
+        want = oracle.price_fp64(book)
+        cpu_s = time.perf_counter() - t0
+        rel = float(np.max(np.abs(got - want) / np.maximum(np.abs(want), 1e-300)))
+        cpu = {"value": n / cpu_s, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{n} options, one pass of the FP64 oracle (the same formula in double)"}
+    value = n * runs * steps / secs
+    return {"workload": f"FP64 map, {n} options, {runs} passes per step", "options": n,
+            "num_runs": runs, "steps": steps, "warmup": warmup,
+            "value": value, "unit": UNIT, "ms_per_step": 1e3 * secs / steps, "dtype": "f64",
             "roofline": {"bound": "fp64 issue", "achieved_GBps": 52 * value / 1e9,
                          "note": "52 B/option would allow ~1.3e11 options/s from HBM; "
                                  "GB300's FP64 rate binds first"},
-            "max_rel_vs_cpu_fp64": (float(np.max(np.abs(got - want) / np.maximum(np.abs(want), 1e-300)))
-                                    if want is not None else None),
-            "gpu_launches": ctx.launches - l0, "clocks": clk.summary()}
+            "max_rel_vs_cpu_fp64": rel, "cpu_baseline": cpu,
+            "gpu_launches": launches, "clocks": clk}
+
+
+def run_fp64(args, rank, world, local):
+    """--config fp64: the FP64 product mode's record as its own JSON line."""
+    import torch
+
+    from p3arsec_gb300 import build as b
+    b.build()
+    torch.cuda.set_device(local)
+    rec = fp64_record(args, local)
+    line = {"metric": "FP64 product mode: options/s (double storage)", "value": rec["value"],
+            "unit": UNIT, "n_gpus": world, "steps": rec["steps"], "warmup": rec["warmup"],
+            "ms_per_step": rec["ms_per_step"], "higher_is_better": True, "dtype": "f64",
+            "data": "synthetic (seeded book widened to double)",
+            "config": {"workload": rec["workload"], "options": rec["options"],
+                       "num_runs": rec["num_runs"]},
+            **{k: rec[k] for k in ("roofline", "max_rel_vs_cpu_fp64", "cpu_baseline",
+                                   "gpu_launches", "clocks")}}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ctx.close()
 
 
 # ---------------------------------------------------------------- file I/O
-def run_io(args, rank, world, local):
+def io_record(args, n=None):
     """The reference's file formats: parallel parse / write of libbsgpu.so vs
     the reference's sequential fscanf / fprintf loops (oracle restatement),
     same files, results checked byte for byte."""
@@ -843,12 +877,8 @@ def run_io(args, rank, world, local):
 
     import oracle
     from p3arsec_gb300 import abi, books
-    from p3arsec_gb300 import build as b
-    b.build()
     oracle.build(ref=False)
-    if rank != 0:
-        return
-    n = args.n
+    n = args.n if n is None else n
     book = books.generate(n, seed=SEED + 7)
     prices = oracle.price_ref(book.slice(0, min(n, 1 << 20)))
     prices = np.resize(prices, n).astype(np.float32)
@@ -884,20 +914,33 @@ def run_io(args, rank, world, local):
             same_out = f1.read() == f2.read()
     finally:
         shutil.rmtree(d, ignore_errors=True)
-    line = {
-        "metric": "PARSEC file I/O: options/s parsed and written (reference formats)",
-        "value": n / best, "unit": UNIT, "n_gpus": 0, "higher_is_better": True,
-        "dtype": "f32", "data": "synthetic (seeded book)",
-        "config": {"workload": f"{n} options: parse a {mb_in:.0f} MB input file, write a "
-                               f"{mb_out:.0f} MB %.18f output file", "threads": threads},
+    return {
+        "workload": f"{n} options: parse a {mb_in:.0f} MB input file, write a "
+                    f"{mb_out:.0f} MB %.18f output file", "options": n, "threads": threads,
+        "value": n / best, "unit": UNIT,
         "parse": {"ours_s": best, "ours_MBps": mb_in / best, "reference_fscanf_s": t_ref,
                   "speedup": t_ref / best, "bit_identical": same_in},
         "write": {"ours_s": bw, "ours_MBps": mb_out / bw, "reference_fprintf_s": t_refw,
                   "speedup": t_refw / bw, "byte_identical": same_out},
         "input_generation_s": t_gen,
         "cpu_baseline": {"value": n / t_ref, "unit": UNIT, "cores": 1, "kind": "port",
-                         "sample": "the reference's fscanf loop (blackscholes.c:726-734) on the same file"},
+                         "sample": "the reference's fscanf loop (blackscholes.c:726-734) on the "
+                                   "same file"},
     }
+
+
+def run_io(args, rank, world, local):
+    """--config io: the file-format record as its own JSON line (host code)."""
+    from p3arsec_gb300 import build as b
+    b.build()
+    if rank != 0:
+        return
+    rec = io_record(args)
+    line = {"metric": "PARSEC file I/O: options/s parsed and written (reference formats)",
+            "value": rec["value"], "unit": UNIT, "n_gpus": 0, "higher_is_better": True,
+            "dtype": "f32", "data": "synthetic (seeded book)",
+            "config": {"workload": rec["workload"], "threads": rec["threads"]},
+            **{k: rec[k] for k in ("parse", "write", "input_generation_s", "cpu_baseline")}}
     print(json.dumps(line), flush=True)
 
 
