@@ -382,6 +382,13 @@ typedef struct bsg_swaption {
 int bsg_price_swaptions(bsg_ctx* ctx, const bsg_swaption* swaptions, size_t n,
                         uint64_t trials, double* price, double* std_err);
 
+/* The normal variates the swaption kernel draws, for given random words:
+ * words[4 i .. 4 i + 3] (host array) -> z[2 i], z[2 i + 1] (host array), by
+ * the device's Box-Muller transform (u1 from words 0-1, u2 from words 2-3,
+ * u = (2k + 1) 2^-53 with k = the top 20 bits of the first word and all of
+ * the second).  For checking the transform against a host evaluation. */
+int bsg_swaption_normals(bsg_ctx* ctx, const uint32_t* words, size_t n_pairs, double* z);
+
 /* The reference's per-swaption signature (HJM_Swaption_Blocking.cpp:19-41;
  * FTYPE = double) on the default context of device 0: pdSwaptionPrice[0] =
  * price, [1] = standard error.  Returns 1 on success as the reference does,

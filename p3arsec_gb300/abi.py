@@ -191,6 +191,7 @@ SIGNATURES = {
     "bsg_get_tune": (_I, [_P, ctypes.POINTER(Tune)]),
     "bsg_set_tune": (_I, [_P, ctypes.POINTER(Tune)]),
     "bsg_price_swaptions": (_I, [_P, ctypes.POINTER(SwaptionC), _SZ, ctypes.c_uint64, _P, _P]),
+    "bsg_swaption_normals": (_I, [_P, _P, _SZ, _P]),
     "bsg_HJM_Swaption_Blocking": (_I, [_P] + [ctypes.c_double] * 5 + [_I, _I, ctypes.c_double,
                                                                        _P, _P, ctypes.c_long,
                                                                        ctypes.c_long, _I, _I]),
@@ -437,6 +438,17 @@ class Context:
         st = self.lib.bsg_price_swaptions(self.h, arr, n, trials, ptr(price), ptr(err))
         _check(self.lib, self.h, st)
         return price, err
+
+    def swaption_normals(self, words):
+        """bsg_swaption_normals: the swaption kernel's normal pairs of the
+        uint32 words (4 per pair); returns float64 z of 2 per pair."""
+        w = np.ascontiguousarray(words, dtype=np.uint32)
+        if w.size % 4:
+            raise ValueError("4 words per pair")
+        z = np.empty(w.size // 2)
+        st = self.lib.bsg_swaption_normals(self.h, ptr(w), w.size // 4, ptr(z))
+        _check(self.lib, self.h, st)
+        return z
 
     def set_tune(self, vec_per_thread=1, block=256, blocks_per_sm=0, load_path=0, pdl=0,
                  resident_32nds=0):

@@ -1301,6 +1301,34 @@ extern "C" int bsg_price_swaptions(bsg_ctx* c, const bsg_swaption* sw, size_t n,
     return BSG_OK;
 }
 
+extern "C" int bsg_swaption_normals(bsg_ctx* c, const uint32_t* words, size_t n_pairs, double* z) {
+    if (!c) return BSG_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (n_pairs == 0) return BSG_OK;
+    if (!words || !z) return fail(c, BSG_ERR_INVALID_ARG, "words or z is NULL");
+    if (n_pairs > ((size_t)1 << 26)) return fail(c, BSG_ERR_CAPACITY, "at most 2^26 pairs per call");
+    BSG_CK(c, cudaSetDevice(c->device));
+    if (int st = drain_pipeline(c)) return st;
+    void* d = nullptr;
+    const size_t wb = n_pairs * 4 * sizeof(uint32_t), zb = n_pairs * 2 * sizeof(double);
+    if (cudaMalloc(&d, wb + zb) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(c, BSG_ERR_OUT_OF_MEMORY, "swaption normals scratch");
+    }
+    uint32_t* dw = static_cast<uint32_t*>(d);
+    double* dz = reinterpret_cast<double*>(static_cast<char*>(d) + wb);  // wb is a multiple of 16
+    cudaError_t e = cudaMemcpyAsync(dw, words, wb, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = bsg::launch_swaption_normals(dw, n_pairs, dz, c->stream);
+    if (e == cudaSuccess) {
+        c->launches += 1;
+        e = cudaMemcpyAsync(z, dz, zb, cudaMemcpyDeviceToHost, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(c, e, "bsg_swaption_normals");
+    return BSG_OK;
+}
+
 extern "C" int bsg_HJM_Swaption_Blocking(double* pdSwaptionPrice, double dStrike,
                                          double dCompounding, double dMaturity, double dTenor,
                                          double dPaymentInterval, int iN, int iFactors,

@@ -168,6 +168,10 @@ int swaption_chunks(uint64_t trials, int per_thread);
 cudaError_t launch_swaptions(const SwParams* prm, int nsw, int max_steps, uint64_t trials,
                              int per_thread, double* partial, double* out, cudaStream_t st);
 
+// z[2 i], z[2 i + 1] = the swaption kernel's normal pair of words[4 i .. 4 i + 3]
+// (device arrays), i < n.
+cudaError_t launch_swaption_normals(const uint32_t* words, uint64_t n, double* z, cudaStream_t st);
+
 // Fills n options with a deterministic plausible book (autotuning input).
 cudaError_t launch_fill(const SoA& a, int64_t n, uint32_t seed, int sm_count,
                         cudaStream_t st);

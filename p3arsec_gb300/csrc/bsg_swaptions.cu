@@ -18,20 +18,27 @@
 // factor k's vols), the drift that makes discounted bonds martingales.
 //
 // Work that cannot reach the payoff is not done: rows of the path after the
-// swaption's maturity t_s (the reference simulates all n_steps - 1 of them)
-// and the discount factors of swap dates without a payment.  The variates of
-// the rows that are simulated are the same ones: each is drawn from a
+// swaption's maturity t_s (the reference simulates all n_steps - 1 of them),
+// the entries of each row that no payment date of the swap reads, and the
+// discount factors of swap dates without a payment.  The variates of the
+// rows that are simulated are the same ones: each is drawn from a
 // counter-based generator (Philox4x32-10, Salmon et al., SC'11) keyed by
-// (seed, trial, index) and turned normal by Box-Muller, so the prices equal
-// those of a full-path simulation with the same stream.
+// (seed, trial, index) and turned normal by Box-Muller (bsg_swnormal.h:
+// table-driven -2 ln u and sin/cos(2 pi u) from the uniforms' bits), so the
+// prices equal those of a full-path simulation with the same stream.  The
+// kernel is bound by GB300's FP64 rate; the trimming and the table-driven
+// transform halve its double-precision work per path.
 //
 // Reduction: each block reduces its paths' sums (sum and sum of squares of
 // the discounted payoff) in a fixed order and writes one partial; a second
 // kernel adds a swaption's partials in a fixed order.  Results do not depend
 // on scheduling: two runs give the same bits.
 #include "bsg_internal.h"
+#include "bsg_swnormal.h"
 
 #include <math.h>
+
+#include <algorithm>
 
 namespace bsg {
 
@@ -59,26 +66,23 @@ __device__ __forceinline__ void philox4x32_10(uint32_t x0, uint32_t x1, uint32_t
     out[3] = x3;
 }
 
-// (0, 1) from 52 random bits k (the top 20 bits of a, all of b): the double
-// 1 + k 2^-52 built from its bits, minus 1, plus 2^-53 -- (2k + 1) 2^-53,
-// both additions exact, two double operations and no conversion.
-__device__ __forceinline__ double unit52(uint32_t a, uint32_t b) {
-    const double d = __hiloint2double((int)(0x3FF00000u | (a >> 12)), (int)b);
-    return __dadd_rn(__dadd_rn(d, -1.0), 1.1102230246251565e-16);
-}
-
-// Normal variates 2j and 2j + 1 of trial t: Box-Muller, the angle 2 pi u2
-// evaluated as sincospi(2 u2) (2 u2 is exact; no reduction by pi needed).
-__device__ __forceinline__ void normal_pair(uint64_t seed, uint64_t t, uint32_t j, double& z0,
-                                            double& z1) {
+// Normal variates 2j and 2j + 1 of trial t: Box-Muller on the uniforms of
+// the Philox block (seed, t, j), evaluated from their bits (bsg_swnormal.h).
+__device__ __forceinline__ void normal_pair(const bsg_sw::Tables& tab, uint64_t seed, uint64_t t,
+                                            uint32_t j, double& z0, double& z1) {
     uint32_t x[4];
     philox4x32_10((uint32_t)t, (uint32_t)(t >> 32), j, 0u, (uint32_t)seed, (uint32_t)(seed >> 32), x);
-    const double u1 = unit52(x[0], x[1]), u2 = unit52(x[2], x[3]);
-    const double r = sqrt(-2.0 * log(u1));
-    double s, c;
-    sincospi(2.0 * u2, &s, &c);
-    z0 = r * c;
-    z1 = r * s;
+    bsg_sw::normal_pair(tab, x[0], x[1], x[2], x[3], &z0, &z1);
+}
+
+__device__ const bsg_sw::Tables kNormalTables = BSG_SW_TABLES;
+
+// Copies the transform's tables into shared memory (all threads of the block).
+__device__ __forceinline__ void load_normal_tables(bsg_sw::Tables& dst) {
+    const double2* src = reinterpret_cast<const double2*>(&kNormalTables);
+    double2* d = reinterpret_cast<double2*>(&dst);
+    for (int i = threadIdx.x; i < (int)(sizeof(bsg_sw::Tables) / sizeof(double2)); i += blockDim.x)
+        d[i] = src[i];
 }
 
 // Per-swaption constants in shared memory: the forward curve, the drift
@@ -90,11 +94,59 @@ struct SwShared {
     double vol[kSwMaxFactors][MAXN];
     double pay[MAXN];
     double red[2][kSwThreads / 32];
+    bsg_sw::Tables nt;
 };
+
+// Paths q * kSwThreads + threadIdx.x (q < per_thread) of one block, with the
+// path rows cut to the NEED entries that reach the payoff (row i of the
+// reference's path computes all n - 1 - i; the others never reach a
+// payment date before the swap's last, so the price is the same).
+template <int MAXN, int NEED>
+__device__ __forceinline__ void price_paths(const SwParams& p, const SwShared<MAXN>& sh, uint64_t base,
+                                            int per_thread, uint64_t trials, double& sum,
+                                            double& sum_sq) {
+    const int s = p.start, nf = p.n_factors, last = p.swap_points;
+    const double h = p.h;
+    for (int q = 0; q < per_thread; ++q) {
+        const uint64_t t = base + (uint64_t)q * kSwThreads + threadIdx.x;
+        if (t >= trials) break;
+        double f[NEED + 1];
+#pragma unroll
+        for (int m = 0; m <= NEED; ++m) f[m] = sh.fwd[m];
+        double acc = 0.0, zc[2] = {0.0, 0.0};
+        int zi = 0;  // index of the next normal variate of this trial
+        for (int i = 0; i < s; ++i) {
+            acc += f[0];
+            double shock[NEED];
+#pragma unroll
+            for (int m = 0; m < NEED; ++m) shock[m] = 0.0;
+            for (int k = 0; k < nf; ++k, ++zi) {
+                if ((zi & 1) == 0) normal_pair(sh.nt, p.seed, t, (uint32_t)(zi >> 1), zc[0], zc[1]);
+                const double z = zc[zi & 1];
+#pragma unroll
+                for (int m = 0; m < NEED; ++m) shock[m] = __fma_rn(sh.vol[k][m], z, shock[m]);
+            }
+            // row i + 1 from row i (entries at or past NEED - i are never read)
+#pragma unroll
+            for (int m = 0; m < NEED; ++m) f[m] = f[m + 1] + sh.muh[m] + shock[m];
+        }
+        const double disc = exp(-acc * h);
+        double fixed = 0.0, accs = 0.0;
+#pragma unroll
+        for (int l = 0; l <= NEED; ++l) {
+            if (l <= last && sh.pay[l] != 0.0) fixed += sh.pay[l] * exp(-accs * h);
+            accs += f[l];
+        }
+        const double payoff = fixed - 1.0 > 0.0 ? fixed - 1.0 : 0.0;
+        const double dp = payoff * disc;
+        sum += dp;
+        sum_sq += dp * dp;
+    }
+}
 
 // One block: paths [chunk * per_block, ...) of swaption blockIdx.y.
 template <int MAXN>
-__global__ void __launch_bounds__(kSwThreads, 2) swaption_paths_kernel(const SwParams* __restrict__ prm,
+__global__ void __launch_bounds__(kSwThreads, MAXN <= 12 ? 2 : 1) swaption_paths_kernel(const SwParams* __restrict__ prm,
                                                                     uint64_t trials, int per_thread,
                                                                     double* __restrict__ partial) {
     __shared__ SwShared<MAXN> sh;
@@ -103,6 +155,7 @@ __global__ void __launch_bounds__(kSwThreads, 2) swaption_paths_kernel(const SwP
     const double h = p.h;
     // set-up, the same in every block of the swaption: forward curve from the
     // yields, drift from the vols, payments (HJM_Swaption_Blocking.cpp:132-140)
+    load_normal_tables(sh.nt);
     if (threadIdx.x < MAXN) {
         const int i = threadIdx.x;
         sh.fwd[i] = i == 0 ? p.yield[0]
@@ -123,43 +176,23 @@ __global__ void __launch_bounds__(kSwThreads, 2) swaption_paths_kernel(const SwP
         sh.muh[i] = mu * h;
     }
     __syncthreads();
-    const int s = p.start, L = p.swap_len;
     const uint64_t base = (uint64_t)blockIdx.x * per_thread * kSwThreads;
     double sum = 0.0, sum_sq = 0.0;
-    for (int q = 0; q < per_thread; ++q) {
-        const uint64_t t = base + (uint64_t)q * kSwThreads + threadIdx.x;
-        if (t >= trials) break;
-        double f[MAXN];
-#pragma unroll
-        for (int m = 0; m < MAXN; ++m) f[m] = sh.fwd[m];
-        double acc = 0.0, zc[2] = {0.0, 0.0};
-        int zi = 0;  // index of the next normal variate of this trial
-        for (int i = 0; i < s; ++i) {
-            acc += f[0];
-            double shock[MAXN];
-#pragma unroll
-            for (int m = 0; m < MAXN; ++m) shock[m] = 0.0;
-            for (int k = 0; k < nf; ++k, ++zi) {
-                if ((zi & 1) == 0) normal_pair(p.seed, t, (uint32_t)(zi >> 1), zc[0], zc[1]);
-                const double z = zc[zi & 1];
-#pragma unroll
-                for (int m = 0; m < MAXN - 1; ++m) shock[m] = __fma_rn(sh.vol[k][m], z, shock[m]);
-            }
-            // row i + 1 from row i (entries past n - 1 - i are never read)
-#pragma unroll
-            for (int m = 0; m < MAXN - 1; ++m) f[m] = f[m + 1] + sh.muh[m] + shock[m];
-        }
-        const double disc = exp(-acc * h);
-        double fixed = 0.0, accs = 0.0;
-#pragma unroll
-        for (int l = 0; l < MAXN; ++l) {
-            if (l < L && sh.pay[l] != 0.0) fixed += sh.pay[l] * exp(-accs * h);
-            accs += f[l];
-        }
-        const double payoff = fixed - 1.0 > 0.0 ? fixed - 1.0 : 0.0;
-        const double dp = payoff * disc;
-        sum += dp;
-        sum_sq += dp * dp;
+    // rows of the path that reach the payoff: row i needs entries
+    // m < swap_points + start - 1 - i (the last payment's discount reads
+    // f[0 .. swap_points - 1] of row start); swap_points + start <= n - 1
+    switch (p.swap_points + p.start - 1) {
+        case 1: price_paths<MAXN, 1>(p, sh, base, per_thread, trials, sum, sum_sq); break;
+        case 2: price_paths<MAXN, 2>(p, sh, base, per_thread, trials, sum, sum_sq); break;
+        case 3: price_paths<MAXN, 3>(p, sh, base, per_thread, trials, sum, sum_sq); break;
+        case 4: price_paths<MAXN, 4>(p, sh, base, per_thread, trials, sum, sum_sq); break;
+        case 5: price_paths<MAXN, 5>(p, sh, base, per_thread, trials, sum, sum_sq); break;
+        case 6: price_paths<MAXN, 6>(p, sh, base, per_thread, trials, sum, sum_sq); break;
+        case 7: price_paths<MAXN, 7>(p, sh, base, per_thread, trials, sum, sum_sq); break;
+        case 8: price_paths<MAXN, 8>(p, sh, base, per_thread, trials, sum, sum_sq); break;
+        case 9: price_paths<MAXN, 9>(p, sh, base, per_thread, trials, sum, sum_sq); break;
+        case 10: price_paths<MAXN, 10>(p, sh, base, per_thread, trials, sum, sum_sq); break;
+        default: price_paths<MAXN, MAXN - 1>(p, sh, base, per_thread, trials, sum, sum_sq); break;
     }
     // block reduction in a fixed order
 #pragma unroll
@@ -212,7 +245,25 @@ __global__ void __launch_bounds__(kSwThreads) swaption_reduce_kernel(const doubl
     }
 }
 
+__global__ void __launch_bounds__(kSwThreads) swaption_normals_kernel(const uint32_t* __restrict__ words,
+                                                                      uint64_t n, double* __restrict__ z) {
+    __shared__ bsg_sw::Tables nt;
+    load_normal_tables(nt);
+    __syncthreads();
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        bsg_sw::normal_pair(nt, words[4 * i], words[4 * i + 1], words[4 * i + 2], words[4 * i + 3],
+                            &z[2 * i], &z[2 * i + 1]);
+}
+
 }  // namespace
+
+cudaError_t launch_swaption_normals(const uint32_t* words, uint64_t n, double* z, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    const uint64_t blocks = std::min<uint64_t>((n + kSwThreads - 1) / kSwThreads, 4096);
+    swaption_normals_kernel<<<(unsigned)blocks, kSwThreads, 0, st>>>(words, n, z);
+    return cudaGetLastError();
+}
 
 int swaption_chunks(uint64_t trials, int per_thread) {
     const uint64_t per_block = (uint64_t)per_thread * kSwThreads;
