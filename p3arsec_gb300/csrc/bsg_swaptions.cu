@@ -23,18 +23,18 @@
 // discount factors of swap dates without a payment.  The variates of the
 // rows that are simulated are the same ones: each is drawn from a
 // counter-based generator (Philox4x32-10, Salmon et al., SC'11) keyed by
-// (seed, trial, index) and turned normal by Box-Muller (bsg_swnormal.h:
+// (seed, trial, index) and turned normal by Box-Muller (bsg_swmath.h:
 // table-driven -2 ln u and sin/cos(2 pi u) from the uniforms' bits), so the
 // prices equal those of a full-path simulation with the same stream.  The
 // kernel is bound by GB300's FP64 rate; the trimming and the table-driven
-// transform halve its double-precision work per path.
+// transform and exp (bsg_swmath.h) halve its double-precision work per path.
 //
 // Reduction: each block reduces its paths' sums (sum and sum of squares of
 // the discounted payoff) in a fixed order and writes one partial; a second
 // kernel adds a swaption's partials in a fixed order.  Results do not depend
 // on scheduling: two runs give the same bits.
 #include "bsg_internal.h"
-#include "bsg_swnormal.h"
+#include "bsg_swmath.h"
 
 #include <math.h>
 
@@ -67,7 +67,7 @@ __device__ __forceinline__ void philox4x32_10(uint32_t x0, uint32_t x1, uint32_t
 }
 
 // Normal variates 2j and 2j + 1 of trial t: Box-Muller on the uniforms of
-// the Philox block (seed, t, j), evaluated from their bits (bsg_swnormal.h).
+// the Philox block (seed, t, j), evaluated from their bits (bsg_swmath.h).
 __device__ __forceinline__ void normal_pair(const bsg_sw::Tables& tab, uint64_t seed, uint64_t t,
                                             uint32_t j, double& z0, double& z1) {
     uint32_t x[4];
@@ -75,11 +75,11 @@ __device__ __forceinline__ void normal_pair(const bsg_sw::Tables& tab, uint64_t 
     bsg_sw::normal_pair(tab, x[0], x[1], x[2], x[3], &z0, &z1);
 }
 
-__device__ const bsg_sw::Tables kNormalTables = BSG_SW_TABLES;
+__device__ const bsg_sw::Tables kSwTables = BSG_SW_TABLES;
 
-// Copies the transform's tables into shared memory (all threads of the block).
-__device__ __forceinline__ void load_normal_tables(bsg_sw::Tables& dst) {
-    const double2* src = reinterpret_cast<const double2*>(&kNormalTables);
+// Copies the tables of bsg_swmath.h into shared memory (all threads of the block).
+__device__ __forceinline__ void load_tables(bsg_sw::Tables& dst) {
+    const double2* src = reinterpret_cast<const double2*>(&kSwTables);
     double2* d = reinterpret_cast<double2*>(&dst);
     for (int i = threadIdx.x; i < (int)(sizeof(bsg_sw::Tables) / sizeof(double2)); i += blockDim.x)
         d[i] = src[i];
@@ -130,11 +130,11 @@ __device__ __forceinline__ void price_paths(const SwParams& p, const SwShared<MA
 #pragma unroll
             for (int m = 0; m < NEED; ++m) f[m] = f[m + 1] + sh.muh[m] + shock[m];
         }
-        const double disc = exp(-acc * h);
+        const double disc = bsg_sw::exp_(sh.nt, -acc * h);
         double fixed = 0.0, accs = 0.0;
 #pragma unroll
         for (int l = 0; l <= NEED; ++l) {
-            if (l <= last && sh.pay[l] != 0.0) fixed += sh.pay[l] * exp(-accs * h);
+            if (l <= last && sh.pay[l] != 0.0) fixed += sh.pay[l] * bsg_sw::exp_(sh.nt, -accs * h);
             accs += f[l];
         }
         const double payoff = fixed - 1.0 > 0.0 ? fixed - 1.0 : 0.0;
@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(kSwThreads, MAXN <= 12 ? 2 : 1) swaption_paths
     const double h = p.h;
     // set-up, the same in every block of the swaption: forward curve from the
     // yields, drift from the vols, payments (HJM_Swaption_Blocking.cpp:132-140)
-    load_normal_tables(sh.nt);
+    load_tables(sh.nt);
     if (threadIdx.x < MAXN) {
         const int i = threadIdx.x;
         sh.fwd[i] = i == 0 ? p.yield[0]
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(kSwThreads) swaption_reduce_kernel(const doubl
 __global__ void __launch_bounds__(kSwThreads) swaption_normals_kernel(const uint32_t* __restrict__ words,
                                                                       uint64_t n, double* __restrict__ z) {
     __shared__ bsg_sw::Tables nt;
-    load_normal_tables(nt);
+    load_tables(nt);
     __syncthreads();
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
          i += (uint64_t)gridDim.x * blockDim.x)

@@ -1,6 +1,7 @@
-// bsg_swnormal.h -- normal variates of the swaption Monte Carlo: Box-Muller
-// evaluated from the bits of the uniforms with table-driven -2 ln u and
-// sin/cos(2 pi u), in double precision.
+// bsg_swmath.h -- double-precision elementary functions of the swaption
+// Monte Carlo: the normal variates (Box-Muller evaluated from the bits of
+// the uniforms with table-driven -2 ln u and sin/cos(2 pi u)) and the
+// exponential of the discount factors.
 //
 // The uniforms are u = (2k + 1) 2^-53 for a 52-bit integer k (the grid of
 // midpoints in (0, 1)); a pair (u1, u2) gives z0 = sqrt(-2 ln u1) cos(2 pi u2)
@@ -20,19 +21,24 @@
 //    x (2 pi 2^-53) (|phi| <= pi/256); the angle-addition formulas combine
 //    the table's sin/cos(2 pi j/256) with Taylor polynomials of sin phi (to
 //    phi^7) and cos phi - 1 (to phi^6).
+//  e^x: x = (64 m + j) ln2/64 + r with k = 64 m + j the integer nearest
+//    64 x / ln 2 (|r| <= ln2/128), e^x = 2^m 2^(j/64) (1 + p(r)), p the
+//    Taylor polynomial of e^r - 1 to r^6; ln2/64 in two parts so that r is
+//    exact to far below its ulp (P. T. P. Tang, ACM TOMS 15(2), 1989).
+//    Arguments of magnitude 700 or more (and NaN) go to the platform's exp.
 //
 // Every operation is an explicitly rounded IEEE double operation (add, mul,
 // fma, sqrt) or integer work, so the host build of this header (compile it
 // with -ffp-contract=off) gives the same bits as the GPU; the CPU test
-// checks the very code the GPU runs.  Errors: -2 ln u and sin/cos within a
-// few ulp of the exact values (the test states the bounds), about half the
-// double-precision work of calling log, sqrt and sincospi on the uniforms.
+// checks the very code the GPU runs.  Errors: within a few ulp of the exact
+// values (the test states the bounds), at about half the double-precision
+// work of calling log, sqrt, sincospi and exp.
 #pragma once
 #include <math.h>
 #include <stdint.h>
 #include <string.h>
 
-#include "bsg_swnormal_tables.h"
+#include "bsg_swmath_tables.h"
 
 #if defined(__CUDACC__)
 #define BSG_SW_FN __host__ __device__ __forceinline__
@@ -45,11 +51,12 @@ namespace bsg_sw {
 struct alignas(16) LogEntry { double neg2_inv_f, neg2_ln_f; };
 struct alignas(16) Angle { double s, c; };
 
-// 6,672 bytes: the kernels copy it into shared memory once per block.
+// 7,184 bytes: the kernels copy it into shared memory once per block.
 struct Tables {
     LogEntry lg[129];
-    double e2[64];  // 2 i ln 2
+    double e2[64];   // 2 i ln 2
     Angle ang[256];
+    double e64[64];  // 2^(j/64)
 };
 
 #if defined(__CUDA_ARCH__)
@@ -59,6 +66,8 @@ BSG_SW_FN double add(double a, double b) { return __dadd_rn(a, b); }
 BSG_SW_FN double sqrt_(double a) { return __dsqrt_rn(a); }
 BSG_SW_FN double from_bits(uint64_t u) { return __longlong_as_double((long long)u); }
 BSG_SW_FN int clz64(uint64_t v) { return __clzll((long long)v); }
+BSG_SW_FN uint64_t to_bits(double d) { return (uint64_t)__double_as_longlong(d); }
+BSG_SW_FN double exp_fallback(double x) { return exp(x); }
 #else
 inline double fma_(double a, double b, double c) { return fma(a, b, c); }
 inline double mul(double a, double b) { return a * b; }
@@ -66,6 +75,8 @@ inline double add(double a, double b) { return a + b; }
 inline double sqrt_(double a) { return sqrt(a); }
 inline double from_bits(uint64_t u) { double d; memcpy(&d, &u, 8); return d; }
 inline int clz64(uint64_t v) { return __builtin_clzll(v); }
+inline uint64_t to_bits(double d) { uint64_t u; memcpy(&u, &d, 8); return u; }
+inline double exp_fallback(double x) { return exp(x); }
 #endif
 
 // The 52-bit integer k of a uniform from two 32-bit random words (the top
@@ -124,7 +135,27 @@ BSG_SW_FN void normal_pair(const Tables& t, uint32_t w0, uint32_t w1, uint32_t w
     *z1 = mul(r, s);
 }
 
+// e^x; for |x| >= 700 or NaN, the platform's exp.
+BSG_SW_FN double exp_(const Tables& t, double x) {
+    if ((to_bits(x) & 0x7FFFFFFFFFFFFFFFull) >= 0x4085E00000000000ull) return exp_fallback(x);  // 700
+    const double tm = fma_(x, BSG_SW_INV_L, 6755399441055744.0);  // 1.5 2^52 + k
+    const double kd = add(tm, -6755399441055744.0);
+    const int k = (int)(uint32_t)to_bits(tm);                      // |k| < 2^16
+    double r = fma_(-kd, BSG_SW_L1, x);
+    r = fma_(-kd, BSG_SW_L2, r);
+    double q = 1.0 / 720;
+    q = fma_(q, r, 1.0 / 120);
+    q = fma_(q, r, 1.0 / 24);
+    q = fma_(q, r, 1.0 / 6);
+    q = fma_(q, r, 0.5);
+    const double p = fma_(mul(r, r), q, r);                        // e^r - 1
+    const double tj = t.e64[k & 63];
+    const double y = fma_(tj, p, tj);                              // in [0.99, 2.01)
+    return from_bits(to_bits(y) + ((uint64_t)(int64_t)(k >> 6) << 52));
+}
+
 }  // namespace bsg_sw
 
 // The tables' initializer: `const bsg_sw::Tables t = BSG_SW_TABLES;`
-#define BSG_SW_TABLES {{BSG_SW_LOG_TABLE}, {BSG_SW_EXP2_TABLE}, {BSG_SW_ANGLE_TABLE}}
+#define BSG_SW_TABLES \
+    {{BSG_SW_LOG_TABLE}, {BSG_SW_EXP2_TABLE}, {BSG_SW_ANGLE_TABLE}, {BSG_SW_EXP_TABLE}}

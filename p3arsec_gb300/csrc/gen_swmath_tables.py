@@ -1,8 +1,8 @@
-"""Writes bsg_swnormal_tables.h: the tables of the table-driven Box-Muller
-transform in bsg_swnormal.h, computed from 70-digit decimal values of ln 2,
-ln F, sin and cos and rounded once to double.
+"""Writes bsg_swmath_tables.h: the tables of the table-driven Box-Muller
+transform and exponential in bsg_swmath.h, computed from 70-digit decimal
+values of ln 2, ln F, sin, cos and 2^(j/64) and rounded once to double.
 
-    python gen_swnormal_tables.py      # rewrites bsg_swnormal_tables.h here
+    python gen_swmath_tables.py      # rewrites bsg_swmath_tables.h here
 
 Every double is written as a hex literal, so the header is exact."""
 import decimal
@@ -76,8 +76,8 @@ def main():
     ln2 = D(2).ln()
     out = []
     w = out.append
-    w("// bsg_swnormal_tables.h -- written by gen_swnormal_tables.py; do not edit.")
-    w("// Tables of the table-driven Box-Muller transform in bsg_swnormal.h.")
+    w("// bsg_swmath_tables.h -- written by gen_swmath_tables.py; do not edit.")
+    w("// Tables of the table-driven Box-Muller transform and exp in bsg_swmath.h.")
     w("#pragma once")
     w("")
     w("// 2 pi 2^-53: the angle of one unit of the 53-bit uniform grid")
@@ -96,13 +96,25 @@ def main():
     for i in range(64):
         w(f"    {hexd(2 * i * ln2)}" + (", \\" if i < 63 else ""))
     w("")
+    w("// exp: 64/ln 2, and ln2/64 = L1 + L2")
+    L = ln2 / 64
+    L1 = f64(L)
+    w(f"#define BSG_SW_INV_L {hexd(1 / L)}")
+    w(f"#define BSG_SW_L1 {hexd(L)}")
+    w(f"#define BSG_SW_L2 {hexd(Fraction(L) - Fraction(L1))}")
+    w("")
+    w("// 2^(j/64), j = 0..63")
+    w("#define BSG_SW_EXP_TABLE \\")
+    for j in range(64):
+        w(f"    {hexd((D(j) / D(64) * ln2).exp())}" + (", \\" if j < 63 else ""))
+    w("")
     w("// {sin, cos}(2 pi j / 256), j = 0..255")
     w("#define BSG_SW_ANGLE_TABLE \\")
     for j in range(256):
         s, c = sin_cos(2 * PI * D(j) / D(256))
         w(f"    {{{hexd(s)}, {hexd(c)}}}" + (", \\" if j < 255 else ""))
     w("")
-    with open(os.path.join(HERE, "bsg_swnormal_tables.h"), "w") as f:
+    with open(os.path.join(HERE, "bsg_swmath_tables.h"), "w") as f:
         f.write("\n".join(out) + "\n")
 
 

@@ -1,15 +1,19 @@
-// CPU check of the table-driven Box-Muller transform of the swaption Monte
-// Carlo (p3arsec_gb300/csrc/bsg_swnormal.h, the same code the GPU runs)
-// against long-double logl/sinl/cosl.
+// CPU check of the swaption Monte Carlo's elementary functions (the
+// table-driven Box-Muller transform and exp of
+// p3arsec_gb300/csrc/bsg_swmath.h, the same code the GPU runs) against
+// long-double logl/sinl/cosl/expl.
 //
-//   swnormal_check walk <n> <seed>
+//   swmath_check walk <n> <seed>
 //       n pseudo-random 52-bit integers (splitmix64) plus the edge cases
 //       (u next to 0 and 1, every table boundary of both functions and
 //       its neighbours); prints one line
-//       "checked <n> log_ulp <a> trig_abs <b> z_rel <c>"
+//       "checked <n> log_ulp <a> trig_abs <b> z_rel <c> exp_ulp <d>"
 //       log_ulp: max |W - (-2 ln u)| / ulp(-2 ln u); trig_abs: max absolute
-//       error of sin and cos; z_rel: max |z - exact| / max(1, |exact|).
-//   swnormal_check pairs <in> <out>
+//       error of sin and cos; z_rel: max |z - exact| / max(1, |exact|);
+//       exp_ulp: max |exp_(x) - e^x| / ulp(e^x) over n arguments in
+//       [-40, 40], n/4 in (-700, 700) and the points k ln2/64 and their
+//       neighbours.
+//   swmath_check pairs <in> <out>
 //       reads 4 x uint32 words per pair from <in>, writes z0, z1 (double)
 //       per pair to <out>: the host side of the GPU bit-identity test.
 #include <cmath>
@@ -19,7 +23,7 @@
 #include <cstring>
 #include <vector>
 
-#include "bsg_swnormal.h"
+#include "bsg_swmath.h"
 
 namespace {
 
@@ -75,7 +79,27 @@ int walk(long n, uint64_t seed) {
         zrel = std::fmax(zrel, (double)(fabsl(z0 - e0) / fmaxl(1.0L, fabsl(e0))));
         zrel = std::fmax(zrel, (double)(fabsl(z1 - e1) / fmaxl(1.0L, fabsl(e1))));
     }
-    printf("checked %zu log_ulp %.4f trig_abs %.4e z_rel %.4e\n", ks.size(), log_ulp, trig, zrel);
+    std::vector<double> xs;
+    for (long i = 0; i < n; ++i) xs.push_back(-40.0 + 80.0 * ((g.next() >> 11) * 0x1.0p-53));
+    for (long i = 0; i < n / 4; ++i) xs.push_back(-699.99 + 1399.98 * ((g.next() >> 11) * 0x1.0p-53));
+    for (double x : {0.0, -0.0, 1e-300, -1e-300, 1e-17, -1e-17, 699.99, -699.99, 1.0, -1.0})
+        xs.push_back(x);
+    const long double l64 = logl(2.0L) / 64;
+    for (long k = -4096; k <= 4096; ++k) {
+        const double x = (double)(k * l64);
+        xs.push_back(x);
+        xs.push_back(std::nextafter(x, INFINITY));
+        xs.push_back(std::nextafter(x, -INFINITY));
+        xs.push_back((double)((k + 0.5L) * l64));  // the rounding boundaries of k
+    }
+    double exp_ulp = 0;
+    for (double x : xs) {
+        const long double ex = expl((long double)x);
+        const double got = bsg_sw::exp_(kT, x);
+        exp_ulp = std::fmax(exp_ulp, (double)(fabsl((long double)got - ex) / ulp((double)ex)));
+    }
+    printf("checked %zu log_ulp %.4f trig_abs %.4e z_rel %.4e exp_ulp %.4f\n", ks.size() + xs.size(),
+           log_ulp, trig, zrel, exp_ulp);
     return 0;
 }
 
@@ -102,6 +126,6 @@ int pairs(const char* in, const char* out) {
 int main(int argc, char** argv) {
     if (argc == 4 && !strcmp(argv[1], "walk")) return walk(atol(argv[2]), strtoull(argv[3], nullptr, 10));
     if (argc == 4 && !strcmp(argv[1], "pairs")) return pairs(argv[2], argv[3]);
-    fprintf(stderr, "usage: swnormal_check walk <n> <seed> | pairs <in> <out>\n");
+    fprintf(stderr, "usage: swmath_check walk <n> <seed> | pairs <in> <out>\n");
     return 2;
 }

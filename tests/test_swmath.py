@@ -1,9 +1,10 @@
-"""The swaption Monte Carlo's normal variates (p3arsec_gb300/csrc/bsg_swnormal.h):
-Box-Muller with table-driven -2 ln u and sin/cos(2 pi u) computed from the
-uniforms' bits.  On the CPU, the host build of the same header against
-long-double logl/sinl/cosl; on the GPU, the device transform against the
-host build, bit for bit, and against a long-double evaluation of the
-textbook formula."""
+"""The swaption Monte Carlo's elementary functions (p3arsec_gb300/csrc/bsg_swmath.h):
+the normal variates (Box-Muller with table-driven -2 ln u and sin/cos(2 pi u)
+computed from the uniforms' bits) and the discount factors' exp.  On the
+CPU, the host build of the same header against long-double
+logl/sinl/cosl/expl; on the GPU, the device transform against the host
+build, bit for bit, and against a long-double evaluation of the textbook
+formula."""
 import os
 import re
 import subprocess
@@ -17,35 +18,37 @@ CSRC = os.path.join(os.path.dirname(HERE), "p3arsec_gb300", "csrc")
 
 @pytest.fixture(scope="module")
 def checker(tmp_path_factory):
-    exe = str(tmp_path_factory.mktemp("swnormal") / "swnormal_check")
+    exe = str(tmp_path_factory.mktemp("swmath") / "swmath_check")
     subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-I", CSRC,
-                    os.path.join(HERE, "swnormal_check.cpp"), "-o", exe], check=True)
+                    os.path.join(HERE, "swmath_check.cpp"), "-o", exe], check=True)
     return exe
 
 
 def test_accuracy_against_long_double(checker):
     """2M random uniforms plus u next to 0 and 1 and every table boundary:
     -2 ln u within 2 ulp, sin and cos within 1.2e-16, the normals within
-    5.2e-16 of max(1, |z|)."""
+    5.2e-16 of max(1, |z|); 2.5M arguments of exp, its reduction's grid
+    points and rounding boundaries among them: within 1.1 ulp."""
     r = subprocess.run([checker, "walk", "2000000", "1"], stdout=subprocess.PIPE,
                        stderr=subprocess.STDOUT, text=True, timeout=300)
     assert r.returncode == 0, r.stdout
-    m = re.search(r"checked (\d+) log_ulp (\S+) trig_abs (\S+) z_rel (\S+)", r.stdout)
-    checked, log_ulp, trig, zrel = int(m.group(1)), *(float(g) for g in m.groups()[1:])
-    assert checked > 2_000_000
+    m = re.search(r"checked (\d+) log_ulp (\S+) trig_abs (\S+) z_rel (\S+) exp_ulp (\S+)", r.stdout)
+    checked, log_ulp, trig, zrel, exp_ulp = int(m.group(1)), *(float(g) for g in m.groups()[1:])
+    assert checked > 4_500_000
     assert log_ulp <= 2.0 and trig <= 1.2e-16 and zrel <= 5.2e-16, r.stdout
+    assert exp_ulp <= 1.1, r.stdout
 
 
 def test_table_header_is_what_the_generator_writes(tmp_path):
-    """bsg_swnormal_tables.h is generated: regenerating it changes nothing."""
+    """bsg_swmath_tables.h is generated: regenerating it changes nothing."""
     import importlib.util
-    spec = importlib.util.spec_from_file_location("gen", os.path.join(CSRC, "gen_swnormal_tables.py"))
+    spec = importlib.util.spec_from_file_location("gen", os.path.join(CSRC, "gen_swmath_tables.py"))
     gen = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(gen)
     gen.HERE = str(tmp_path)
     gen.main()
-    with open(os.path.join(CSRC, "bsg_swnormal_tables.h")) as a, \
-            open(tmp_path / "bsg_swnormal_tables.h") as b:
+    with open(os.path.join(CSRC, "bsg_swmath_tables.h")) as a, \
+            open(tmp_path / "bsg_swmath_tables.h") as b:
         assert a.read() == b.read()
 
 
