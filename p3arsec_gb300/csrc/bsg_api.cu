@@ -1263,11 +1263,11 @@ extern "C" int bsg_price_swaptions(bsg_ctx* c, const bsg_swaption* sw, size_t n,
     BSG_CK(c, cudaSetDevice(c->device));
     if (int st = drain_pipeline(c)) return st;
     // paths per thread: the most (up to 32; each block pays a set-up) that
-    // still leave 2432 blocks, eight waves of 2 blocks on 152 SMs.  A fixed
+    // still leave 1216 blocks, four waves of 2 blocks on 152 SMs.  A fixed
     // rule of (n, trials), so the summation order -- and the bits -- do
     // not depend on the device.
     int per_thread = 32;
-    while (per_thread > 1 && n * (size_t)bsg::swaption_chunks(trials, per_thread) < 2432) per_thread /= 2;
+    while (per_thread > 1 && n * (size_t)bsg::swaption_chunks(trials, per_thread) < 1216) per_thread /= 2;
     const size_t chunks = (size_t)bsg::swaption_chunks(trials, per_thread);
     const size_t tab_b = round_up(n * sizeof(bsg::SwParams), 256);
     const size_t part_b = round_up(2 * n * chunks * sizeof(double), 256);
