@@ -50,6 +50,34 @@ def test_longer_grids_and_other_factor_counts(gpu_ctx, oracle_lib):
         check(got[i:i + 1], err[i:i + 1], np.array([p]), np.array([e]))
 
 
+def _shaped(n, years, maturity, tenor, pay, i, nf=3):
+    rng = np.random.default_rng(100 + i)
+    return S.Swaption(strike=0.04 + 0.01 * i, years=years, maturity=maturity, tenor=tenor,
+                      payment_interval=pay, yield_curve=0.03 + 0.001 * np.arange(n),
+                      factors=rng.uniform(-0.003, 0.01, (nf, n - 1)), seed=900 + i)
+
+
+@pytest.mark.parametrize("shapes", [
+    # 11- and 12-point grids (the 12-point kernel): rows of every length the
+    # payoff can read there, swap_points + start - 1 = 1..10
+    [(11, 11, 1, 1, 1), (11, 11, 1, 2, 1), (11, 11, 2, 2, 1), (11, 11, 2, 3, 1), (11, 11, 3, 3, 1),
+     (11, 11, 3, 4, 1), (11, 11, 4, 4, 1), (11, 11, 4, 5, 1), (12, 6, 2, 3, 0.5), (12, 12, 1, 10, 1),
+     (11, 5.5, 4.5, 0.5, 0.5)],
+    # with 32-point grids (the 32-point kernel): short rows, and rows longer
+    # than 10 that take the untrimmed body
+    [(32, 16, 0.5, 1, 0.5), (20, 10, 2, 3, 0.5), (32, 8, 2, 3, 0.25), (32, 32, 5, 20, 1)],
+], ids=["12-point", "32-point"])
+def test_every_row_length_against_oracle(gpu_ctx, oracle_lib, shapes):
+    """The kernel cuts each path row to the entries the payoff reads, with
+    one instantiation per row length: every length prices as the oracle's
+    full-matrix simulation of the same paths."""
+    sw = [_shaped(*sh, i) for i, sh in enumerate(shapes)]
+    got, err = gpu_ctx.price_swaptions(sw, 20_000)
+    for i, w in enumerate(sw):
+        p, e = oracle_lib.swaption_price(w, 20_000)
+        check(got[i:i + 1], err[i:i + 1], np.array([p]), np.array([e]))
+
+
 def test_zero_volatility_is_deterministic(gpu_ctx, oracle_lib):
     sw = [S.Swaption(strike=k, years=y, factors=np.zeros((3, 10)), seed=5)
           for k, y in ((0.1, 5.0), (1.7, 12.25), (4.9, 19.75))]
