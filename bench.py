@@ -25,7 +25,7 @@ records measured in the same run:
   the reference's fscanf / fprintf loops.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--config map|batch|precision|serve|io|fp64|prefix-sweep|swaptions]
+                    [--config map|batch|precision|serve|serve-blocks|io|fp64|prefix-sweep|swaptions]
 
 One JSON line on stdout (rank 0).  Under torchrun each rank prices its own
 book on its own GPU (weak scaling, no collective on the data path); the
@@ -679,7 +679,8 @@ def serve_point(host, out, mode, rate, seconds, args, local, seed, sizes=None):
                            max_inflight=args.serve_inflight, plain=(mode == "plain"),
                            drain_timeout_s=60.0,
                            fused=(mode == "batched" and args.serve_fused >= 1),
-                           persistent=(mode == "batched" and args.serve_fused == 2))
+                           persistent=(mode == "batched" and args.serve_fused == 2),
+                           persistent_blocks=args.serve_blocks)
 
 
 def serve_record(args, local, repeats=3, trace_rate=20000.0, trace_seconds=5.0,
@@ -794,6 +795,36 @@ def run_serve(args, rank, world, local):
                                    "host_link", "roofline", "sweep")}}
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def run_serve_blocks(args, rank, world, local):
+    """--config serve-blocks: the persistent kernel's grid size against the
+    batched loop's throughput and latency (one trace per rate and size)."""
+    import torch
+
+    from p3arsec_gb300 import build as b
+    b.build()
+    torch.cuda.set_device(local)
+    if rank != 0:
+        return
+    host, out = serve_host_pool(local)
+    rates = [float(x) for x in args.serve_block_rates.split(",")]
+    rows = []
+    for blocks in (int(x) for x in args.serve_block_list.split(",")):
+        args.serve_blocks = blocks
+        for rate in rates:
+            r = serve_point(host, out, "batched", rate, args.serve_seconds, args, local,
+                            SEED + int(rate))
+            rows.append({"blocks": blocks or "default", "rate_per_s": rate,
+                         "options_per_s": r["options_per_s"], "p50_ms": 1e3 * r["p50_s"],
+                         "p99_ms": 1e3 * r["p99_s"], "p999_ms": 1e3 * r["p999_s"]})
+            print(json.dumps(rows[-1]), file=sys.stderr, flush=True)
+    print(json.dumps({"metric": "persistent serving kernel: grid size vs throughput and latency",
+                      "unit": UNIT, "n_gpus": world, "higher_is_better": True, "dtype": "f32",
+                      "data": "synthetic (seeded trace)",
+                      "config": {"workload": f"open-loop Poisson traces of {args.serve_seconds:g} s, "
+                                             f"sizes log-uniform in [{args.serve_sizes}]"},
+                      "rows": rows}), flush=True)
 
 
 # --------------------------------------------------------- FP64 product mode
@@ -1122,8 +1153,8 @@ def main(argv=None):
                     help="timed steps (default: 100 for the map, 10 otherwise)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=["map", "batch", "precision", "serve", "io", "fp64",
-                                         "prefix-sweep", "swaptions"],
+    ap.add_argument("--config", choices=["map", "batch", "precision", "serve", "serve-blocks", "io",
+                                         "fp64", "prefix-sweep", "swaptions"],
                     default="map")
     ap.add_argument("--serve-rate", type=float, default=20000.0,
                     help="serve: arrival rate of the specified trace (req/s)")
@@ -1141,6 +1172,12 @@ def main(argv=None):
     ap.add_argument("--serve-fused", type=int, default=2,
                     help="2: the persistent kernel; 1: one fused kernel per batch; "
                          "0: gather, price, scatter")
+    ap.add_argument("--serve-blocks", type=int, default=0,
+                    help="serve: blocks of the persistent kernel (0 = SMs x min(occupancy, 3))")
+    ap.add_argument("--serve-block-list", default="16,32,64,128,0",
+                    help="serve-blocks config: the persistent kernel's grid sizes to sweep")
+    ap.add_argument("--serve-block-rates", default="20000,60000,70000,80000",
+                    help="serve-blocks config: arrival rates per grid size")
     ap.add_argument("--books", type=int, default=4096, help="batch config: number of books")
     ap.add_argument("--batch-tune", default=None,
                     help="batch config: tile_options,blocks_per_sm instead of autotuning")
@@ -1180,6 +1217,8 @@ def main(argv=None):
         run_precision(args, rank, world, local)
     elif args.config == "serve":
         run_serve(args, rank, world, local)
+    elif args.config == "serve-blocks":
+        run_serve_blocks(args, rank, world, local)
     elif args.config == "io":
         run_io(args, rank, world, local)
     elif args.config == "fp64":

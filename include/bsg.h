@@ -264,6 +264,8 @@ typedef struct bsg_server_config {
                                  back (the pool then only accounts the budget);
                                  2 = the persistent kernel (no device pool);
                                  0 = gather into the pool, price, scatter */
+    int persistent_blocks;    /* fused = 2: blocks of the persistent kernel,
+                                 8..4096 (0 = SMs x min(occupancy, 3)) */
 } bsg_server_config;
 
 typedef struct bsg_request {

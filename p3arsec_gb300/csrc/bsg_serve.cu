@@ -1167,7 +1167,8 @@ int bsg_server_create(bsg_server** out, const bsg_server_config* cfg) {
     if (!out || !cfg) return BSG_ERR_INVALID_ARG;
     *out = nullptr;
     if (cfg->max_inflight < 1 || cfg->max_inflight > 16 || cfg->max_batch_requests < 0 ||
-        cfg->max_batch_requests > 65536 || cfg->budget_bytes < 28 * kAlign)
+        cfg->max_batch_requests > 65536 || cfg->budget_bytes < 28 * kAlign ||
+        (cfg->persistent_blocks != 0 && (cfg->persistent_blocks < 8 || cfg->persistent_blocks > 4096)))
         return BSG_ERR_INVALID_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || cfg->device < 0 || cfg->device >= ndev) {
@@ -1239,7 +1240,11 @@ int bsg_server_create(bsg_server** out, const bsg_server_config* cfg) {
             if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, serve_persistent_kernel<bsg::MODE_FAST>,
                                                               kThreads, 0) != cudaSuccess || occ < 1)
                 occ = 1;
-            s->pgrid = (unsigned)(s->sm_count * std::min(occ, 3));
+            // enough blocks to keep the host link busy: each block has one
+            // 2048-option tile (49 KB) in flight, and a tile takes ~10 us
+            // on a loaded link, so the link needs ~40+ blocks; 3 per SM
+            s->pgrid = cfg->persistent_blocks ? (unsigned)cfg->persistent_blocks
+                                              : (unsigned)(s->sm_count * std::min(occ, 3));
             break;  // no device pool and no batch slots on this path
         }
         // the device pool holds requests only on the unfused and plain paths;
