@@ -16,6 +16,13 @@
  *    to max_options options, cached CUDA graphs and the tuning choice.  Calls
  *    on one context are serialised by a lock; use one context per host
  *    thread for concurrency.
+ *  - The context's stream is non-blocking: it does not wait for work other
+ *    streams have enqueued (the legacy default stream included).  Device
+ *    arrays passed to a call must be complete when the call is made:
+ *    synchronise their producer first, or produce them on bsg_stream()
+ *    (e.g. torch.cuda.ExternalStream(bsg_stream(ctx))).  A synchronous
+ *    call's results are complete when it returns; a BSG_ASYNC call's after
+ *    bsg_synchronize() or in work ordered after bsg_stream().
  *  - No call ever falls back to a CPU computation: without a usable GPU,
  *    bsg_create fails with BSG_ERR_NO_DEVICE.
  */

@@ -35,6 +35,7 @@ def test_batch_equals_per_book_and_plain(gpu_ctx, seed):
     pool = pool_on_device(torch, book)
     out_b = torch.full((pool_len,), -1.0, device="cuda:0")
     out_p = torch.full((pool_len,), -1.0, device="cuda:0")
+    torch.cuda.synchronize()  # torch's copies and fills are done before the context's stream runs
     gpu_ctx.price_batch(pool[:6], out_b, pool_len, segs, num_runs=1)
     gpu_ctx.price_batch(pool[:6], out_p, pool_len, segs, num_runs=1, plain=True)
     torch.cuda.synchronize()
@@ -56,6 +57,7 @@ def test_batch_graph_runs_and_reuse(gpu_ctx):
     book = books.generate(pool_len, seed=7)
     pool = pool_on_device(torch, book)
     out = torch.zeros(pool_len, device="cuda:0")
+    torch.cuda.synchronize()  # torch's copies and fills are done before the context's stream runs
     for runs in (1, 100, 100, 3):
         gpu_ctx.price_batch(pool, out, pool_len, segs, num_runs=runs)
     torch.cuda.synchronize()
@@ -70,6 +72,7 @@ def test_batch_rejects_bad_segments(gpu_ctx):
     book = books.generate(1000, seed=8)
     pool = pool_on_device(torch, book)
     out = torch.zeros(1000, device="cuda:0")
+    torch.cuda.synchronize()  # torch's copies and fills are done before the context's stream runs
     with pytest.raises(BsgError):
         gpu_ctx.price_batch(pool, out, 1000, [(990, 20)])
     with pytest.raises(BsgError):
@@ -86,6 +89,7 @@ def test_error_report_matches_cpu(gpu_ctx, dist):
     pool = pool_on_device(torch, book)
     prices = gpu_ctx.price_book(book)
     dprices = torch.from_numpy(prices).cuda()
+    torch.cuda.synchronize()  # torch's copies and fills are done before the context's stream runs
     edges = np.array([0.0, 0.5, 1.0, 2.0, 3.0, 4.0, 6.0, np.inf])
     rep = gpu_ctx.error_report(pool, dprices, len(book), edges, rel_floor=1e-3)
     fp64 = oracle.price_fp64(book)
@@ -110,6 +114,7 @@ def test_batch_autotune_and_every_shape_gives_the_same_bits(gpu_ctx):
     book = books.generate(pool_len, seed=12)
     pool = pool_on_device(torch, book)
     out = torch.zeros(pool_len, device="cuda:0")
+    torch.cuda.synchronize()  # torch's copies and fills are done before the context's stream runs
     saved = gpu_ctx.get_batch_tune()
     try:
         chosen = gpu_ctx.autotune_batch(pool, out, pool_len, segs)
@@ -119,6 +124,7 @@ def test_batch_autotune_and_every_shape_gives_the_same_bits(gpu_ctx):
             for bps in (1, 0):
                 gpu_ctx.set_batch_tune(tile, bps)
                 out.zero_()
+                torch.cuda.synchronize()
                 gpu_ctx.price_batch(pool, out, pool_len, segs, num_runs=2)
                 torch.cuda.synchronize()
                 got = out.cpu().numpy()

@@ -57,12 +57,14 @@ def test_bandwidth_size_10m_device_pointers_every_pass_writes_the_same(oracle_li
     book = books.generate(n, seed=7)
     dev = [torch.from_numpy(a).cuda() for a in book.arrays()]
     out = torch.full((n,), -1.0, device="cuda:0")
+    torch.cuda.synchronize()  # torch's copies and fills are done before the context's stream runs
     with Context(0, 1) as ctx:
         ctx.autotune(n)
         ctx.price_soa(*dev, out, n=n, num_runs=100, device=True)
         torch.cuda.synchronize()
         got100 = out.cpu().numpy()
         out.fill_(-1.0)
+        torch.cuda.synchronize()
         ctx.price_soa(*dev, out, n=n, num_runs=1, device=True)
         torch.cuda.synchronize()
         got1 = out.cpu().numpy()

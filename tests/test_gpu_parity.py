@@ -149,6 +149,7 @@ def test_device_pointers_and_misaligned_scalar_path(gpu_ctx, mode):
         d = _dev(torch, book, pad)
         out = torch.zeros(len(book) + pad, dtype=torch.float32, device="cuda:0")
         views = [x[pad:] for x in d]
+        torch.cuda.synchronize()  # torch's copies and fills are done before the context's stream runs
         gpu_ctx.price_soa(*views, out[pad:], n=len(book), num_runs=2, mode=mode, device=True)
         torch.cuda.synchronize()
         got = out[pad:].cpu().numpy()
@@ -223,6 +224,7 @@ def test_out_of_range_device_arguments_are_errors(gpu_ctx):
     book = books.generate(1000, seed=15)
     d = _dev(torch, book)
     out = torch.zeros(1000, dtype=torch.float32, device="cuda:0")
+    torch.cuda.synchronize()  # torch's copies and fills are done before the context's stream runs
     with pytest.raises(BsgError) as e:
         gpu_ctx.price_soa(*d, out, n=1000 + (1 << 30), device=True)
     assert e.value.status == -1
@@ -274,6 +276,7 @@ def test_fp64_product_mode_device_pointers(gpu_ctx):
     wide = [torch.from_numpy(a).cuda() for a in oracle.widened(book)]
     ot = torch.from_numpy(book.otype).cuda()
     out = torch.empty(len(book), dtype=torch.float64, device="cuda:0")
+    torch.cuda.synchronize()  # torch's copies and fills are done before the context's stream runs
     gpu_ctx.price_soa_f64(*wide, ot, out, n=len(book), device=True)
     torch.cuda.synchronize()
     want = oracle.price_fp64(book)

@@ -42,6 +42,7 @@ def _run_pair(gpu_ctx, torch, seed, nseg, max_len, oracle_lib=None):
     pool = [torch.from_numpy(a).cuda() for a in book.arrays()]
     want = torch.full((pool_len,), -1.0, device="cuda:0")
     got = torch.full((pool_len,), -1.0, device="cuda:0")
+    torch.cuda.synchronize()  # torch's copies and fills are done before the context's stream runs
     gpu_ctx.price_batch(pool, want, pool_len, segs)
     torch.cuda.synchronize()
     st = abi.price_batch_noalloc(pool, got, pool_len, segs,
@@ -86,6 +87,7 @@ def test_noalloc_async_calls_queued_back_to_back(gpu_ctx):
         book = books.generate(pool_len, seed=seed)
         pool = [torch.from_numpy(a).cuda() for a in book.arrays()]
         want = torch.full((pool_len,), -1.0, device="cuda:0")
+        torch.cuda.synchronize()  # torch's copies and fills are done before the context's stream runs
         gpu_ctx.price_batch(pool, want, pool_len, segs)
         got = torch.full((pool_len,), -1.0, device="cuda:0")
         cases.append((segs, pool_len, pool, want, got))
@@ -116,6 +118,7 @@ _EXPANDABLE = textwrap.dedent("""
     want = torch.full((n,), -1.0, device="cuda:0")
     segs = [(0, 5_000_001), (5_000_064, n - 5_000_064)]
     st = abi.price_batch_noalloc(pool, got, n, segs)
+    torch.cuda.synchronize()  # torch's copies and fills are done before the context's stream runs
     with Context(0, 1) as ctx:
         ctx.price_batch(pool, want, n, segs)
     torch.cuda.synchronize()
