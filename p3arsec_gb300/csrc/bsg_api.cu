@@ -329,7 +329,7 @@ GraphKey make_key(const bsg::SoA& a, int64_t n, int runs, int mode,
                   const bsg::MapCfg& cfg, int kind, uint64_t ntiles, int nseg,
                   uint64_t btile = 0, int bgrid = 0) {
     GraphKey k;
-    std::memset(&k, 0, sizeof(k));  // padding must compare equal
+    std::memset(static_cast<void*>(&k), 0, sizeof(k));  // padding must compare equal
     k.soa = a;
     k.n = n;
     k.runs = runs;
