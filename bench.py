@@ -177,19 +177,22 @@ def measured_hbm_peak():
 
 # -------------------------------------------------------------- CPU baseline
 PORT_NOTE = ("the oracle port of the reference's FastFlow map (blackscholes.c:315-348): the "
-             "reference's FP32 arithmetic bit for bit, FastFlow's static partition, a join per "
-             "pass, on this host's cores; the reference's own build needs its source tree, which "
-             "is not on this host")
+             "reference's FP32 arithmetic, FastFlow's static partition, a join per pass, on this "
+             "host's cores, compiled as PARSEC compiles the reference (gcc.bldconf:74-75: -O3 "
+             "-funroll-loops -fprefetch-loop-arrays, the compiler's default contraction, so on "
+             "aarch64 with fused multiply-adds as a native build would); the reference's own "
+             "build needs its source tree, which is not on this host")
 
 
 def cpu_baseline(book, target_s: float = 10.0):
-    """The oracle port of the reference's FastFlow map on every host core,
-    over the same book, with as many passes as fit in ~target_s seconds."""
+    """The oracle port of the reference's FastFlow map, built with PARSEC's
+    flags, on every host core, over the same book, with as many passes as
+    fit in ~target_s seconds."""
     import oracle
     threads = os.cpu_count() or 1
-    _, t1 = oracle.bs_map(book, threads, 1)
+    _, t1 = oracle.bs_map(book, threads, 1, parsec_flags=True)
     runs = int(max(1, min(NUM_RUNS, target_s / max(t1, 1e-6))))
-    _, secs = oracle.bs_map(book, threads, runs)
+    _, secs = oracle.bs_map(book, threads, runs, parsec_flags=True)
     return {"value": len(book) * runs / secs, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{len(book)} options x {runs} passes (of {NUM_RUNS}) of the same book, "
                       f"static partition over {threads} threads, {secs:.2f} s",
@@ -1115,9 +1118,9 @@ def run_prefix_sweep(args, rank, world, local):
 
 # ---------------------------------------------------------- reference arm
 def run_reference(args, rank, world, local):
-    """The reference's CPU path (the oracle port of its FastFlow map: same
-    arithmetic bit for bit, static partition, a join per pass) on every host
-    core.  Rank 0 only; other ranks exit without work."""
+    """The reference's CPU path (the oracle port of its FastFlow map: its
+    arithmetic, static partition, a join per pass, built with PARSEC's
+    flags) on every host core.  Rank 0 only; other ranks exit without work."""
     if rank != 0:
         return
     import oracle
@@ -1126,15 +1129,15 @@ def run_reference(args, rank, world, local):
     n = args.n
     book = books.generate(n, seed=SEED)
     threads = os.cpu_count() or 1
-    _, t1 = oracle.bs_map(book, threads, 1)
+    _, t1 = oracle.bs_map(book, threads, 1, parsec_flags=True)
     # each step a bounded sample: ~2 s of CPU work, less when many steps are
     # asked for, so that the whole run stays near a minute
     runs = int(max(1, min(args.runs, round(min(2.0, 60.0 / args.steps) / max(t1, 1e-6)))))
     for _ in range(args.warmup):
-        oracle.bs_map(book, threads, runs)
+        oracle.bs_map(book, threads, runs, parsec_flags=True)
     total = 0.0
     for _ in range(args.steps):
-        _, s = oracle.bs_map(book, threads, runs)
+        _, s = oracle.bs_map(book, threads, runs, parsec_flags=True)
         total += s
     value = n * runs * args.steps / total
     sample = (f"each step {n} options x {runs} passes (of {NUM_RUNS}) on {threads} threads")

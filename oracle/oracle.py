@@ -210,11 +210,34 @@ def write_prices_fprintf(path, prices):
         raise RuntimeError(f"cannot write {path}")
 
 
-def bs_map(book, nthreads: int, num_runs: int):
-    """The threaded NUM_RUNS map driver; returns (prices, roi_seconds)."""
+_parsec = None
+
+
+def _parsec_lib() -> ctypes.CDLL:
+    """libbsoracle_parsec.so: bs_oracle.c built with PARSEC's flags."""
+    global _parsec
+    if _parsec is None:
+        so = os.path.join(HERE, "libbsoracle_parsec.so")
+        if not os.path.exists(so) or os.path.getmtime(so) < os.path.getmtime(
+                os.path.join(HERE, "bs_oracle.c")):
+            build(ref=False)
+        L = ctypes.CDLL(so)
+        L.bso_bs_map.restype = ctypes.c_double
+        L.bso_bs_map.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_size_t] + [_P] * 7
+        _parsec = L
+    return _parsec
+
+
+def bs_map(book, nthreads: int, num_runs: int, parsec_flags: bool = False):
+    """The threaded NUM_RUNS map driver; returns (prices, roi_seconds).
+    parsec_flags: the build with PARSEC's compiler flags (-O3 -funroll-loops
+    -fprefetch-loop-arrays, default contraction), as the reference is built
+    -- the timed CPU baseline; its prices may differ from the checker's by
+    fused multiply-adds on aarch64."""
     a = _arrs(book)
     out = np.empty(len(book), dtype=np.float32)
-    secs = lib().bso_bs_map(nthreads, num_runs, len(book), *[_p(x) for x in a], _p(out))
+    L = _parsec_lib() if parsec_flags else lib()
+    secs = L.bso_bs_map(nthreads, num_runs, len(book), *[_p(x) for x in a], _p(out))
     if secs < 0:
         raise RuntimeError("bso_bs_map failed")
     return out, secs

@@ -81,6 +81,21 @@ def test_threaded_map_equals_serial(oracle_lib, nthreads):
     assert np.array_equal(got.view(np.uint32), serial.view(np.uint32))
 
 
+def test_parsec_flags_build_prices_like_the_checker(oracle_lib):
+    """The timed CPU baseline is the same restatement built with PARSEC's
+    flags and the compiler's default contraction: bit-identical to the
+    checker on x86-64 (no fused multiply-add there), within the reference's
+    1e-4 check (blackscholes.c:333-339) where the compiler fuses."""
+    import platform
+    book = books.generate(200003, seed=23)
+    chk, _ = oracle_lib.bs_map(book, 4, 1)
+    got, secs = oracle_lib.bs_map(book, 4, 2, parsec_flags=True)
+    assert secs >= 0
+    if platform.machine() in ("x86_64", "AMD64"):
+        assert np.array_equal(got.view(np.uint32), chk.view(np.uint32))
+    assert np.abs(got.astype(np.float64) - chk).max() <= 1e-4
+
+
 def test_threaded_map_empty_and_more_threads_than_options(oracle_lib):
     book = books.generate(0, seed=1)
     out, secs = oracle_lib.bs_map(book, 4, 2)
