@@ -686,6 +686,37 @@ def serve_point(host, out, mode, rate, seconds, args, local, seed, sizes=None):
                            persistent_blocks=args.serve_blocks)
 
 
+def equal_p99(sweep, bounds_ms, link_opts):
+    """Throughput at equal p99: for each bound, each loop's best median
+    throughput among the swept rates whose traces all completed with median
+    p99 within the bound; their ratio, and the ceiling the host link puts on
+    it (link options/s over the plain loop's figure).  A loop that meets a
+    bound at no rate gets a note with its median p99 at the lowest rate, and
+    the ratio is null."""
+    def best(mode, bound_ms):
+        ok = [p for p in sweep[mode] if p["all_completed"] and p["median_p99_ms"] <= bound_ms]
+        return max(ok, key=lambda p: p["median_options_per_s"]) if ok else None
+
+    equal = []
+    for bound in bounds_ms:
+        bb, pp = best("batched", bound), best("plain", bound)
+        equal.append({
+            "p99_bound_ms": bound,
+            "batched_options_per_s": bb["median_options_per_s"] if bb else None,
+            "batched_rate_per_s": bb["rate_per_s"] if bb else None,
+            "plain_options_per_s": pp["median_options_per_s"] if pp else None,
+            "plain_rate_per_s": pp["rate_per_s"] if pp else None,
+            "ratio": (bb["median_options_per_s"] / pp["median_options_per_s"]) if (bb and pp) else None,
+            "ratio_ceiling_from_link": (link_opts / pp["median_options_per_s"]) if pp else None})
+        for loop, got in (("plain", pp), ("batched", bb)):
+            if not got:
+                low = min(sweep[loop], key=lambda p: p["rate_per_s"])
+                equal[-1][f"{loop}_note"] = (
+                    f"the {loop} loop's median p99 exceeded {bound:g} ms at every swept rate "
+                    f"(lowest {low['rate_per_s']:g} req/s: {low['median_p99_ms']:.2f} ms)")
+    return equal
+
+
 def serve_record(args, local, repeats=3, trace_rate=20000.0, trace_seconds=5.0,
                  batched_rates=(50000, 55000, 60000, 65000, 70000, 75000, 80000),
                  plain_rates=(500, 1000, 2500, 5000, 7500, 10000, 12500, 15000)):
@@ -726,10 +757,6 @@ def serve_record(args, local, repeats=3, trace_rate=20000.0, trace_seconds=5.0,
                         "all_completed": ok})
         sweep[mode] = pts
 
-    def best(mode, bound_ms):
-        ok = [p for p in sweep[mode] if p["all_completed"] and p["median_p99_ms"] <= bound_ms]
-        return max(ok, key=lambda p: p["median_options_per_s"]) if ok else None
-
     link = host_link_bandwidth(local)
     link_opts = link["h2d_GBps"] * 1e9 / 24
     # one request's own time: 2^20-option requests, one at a time (500/s),
@@ -740,23 +767,7 @@ def serve_record(args, local, repeats=3, trace_rate=20000.0, trace_seconds=5.0,
     single = {m: {"p50_ms": 1e3 * r["p50_s"], "p99_ms": 1e3 * r["p99_s"]} for m, r in alone.items()}
     single["link_alone_ms"] = 1e3 * (24 * big / (link["h2d_GBps"] * 1e9) +
                                      4 * big / (link["d2h_GBps"] * 1e9))
-    equal = []
-    for bound in SERVE_BOUNDS_MS:
-        bb, pp = best("batched", bound), best("plain", bound)
-        equal.append({
-            "p99_bound_ms": bound,
-            "batched_options_per_s": bb["median_options_per_s"] if bb else None,
-            "batched_rate_per_s": bb["rate_per_s"] if bb else None,
-            "plain_options_per_s": pp["median_options_per_s"] if pp else None,
-            "plain_rate_per_s": pp["rate_per_s"] if pp else None,
-            "ratio": (bb["median_options_per_s"] / pp["median_options_per_s"]) if (bb and pp) else None,
-            "ratio_ceiling_from_link": (link_opts / pp["median_options_per_s"]) if pp else None})
-        for loop, got in (("plain", pp), ("batched", bb)):
-            if not got:
-                low = min(sweep[loop], key=lambda p: p["rate_per_s"])
-                equal[-1][f"{loop}_note"] = (
-                    f"the {loop} loop's median p99 exceeded {bound:g} ms at every swept rate "
-                    f"(lowest {low['rate_per_s']:g} req/s: {low['median_p99_ms']:.2f} ms)")
+    equal = equal_p99(sweep, SERVE_BOUNDS_MS, link_opts)
     sat = max(p["median_options_per_s"] for p in sweep["batched"])
     return {
         "workload": f"open-loop Poisson trace at {trace_rate:g} req/s for {trace_seconds:g} s, "

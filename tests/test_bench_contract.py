@@ -79,3 +79,25 @@ def test_prefix_bytes_follows_the_library_rule():
     assert bench.prefix_bytes({"load_path": 2}, 10_000_000, l2) == 0
     assert bench.prefix_bytes(tune, 1000, l2) == 1000 // 8 * 8 * 28  # the whole (small) book
 
+
+
+def _pt(rate, p99, ops, done=True):
+    return {"rate_per_s": rate, "median_p99_ms": p99, "median_options_per_s": ops,
+            "all_completed": done}
+
+
+def test_equal_p99_picks_the_best_rate_within_each_bound():
+    import bench
+    sweep = {"batched": [_pt(50e3, 0.4, 5e9), _pt(60e3, 0.9, 6e9), _pt(70e3, 1.6, 7e9),
+                         _pt(80e3, 1.9, 7.5e9, done=False)],   # a trace that did not drain
+             "plain": [_pt(1e3, 0.7, 1e8), _pt(5e3, 0.95, 5e8), _pt(10e3, 3.0, 9e8)]}
+    eq = {e["p99_bound_ms"]: e for e in bench.equal_p99(sweep, (0.5, 1.0, 2.0), 8.8e9)}
+    # 1 ms: batched 60k (6e9), plain 5k (5e8)
+    assert eq[1.0]["batched_rate_per_s"] == 60e3 and eq[1.0]["plain_rate_per_s"] == 5e3
+    assert eq[1.0]["ratio"] == 6e9 / 5e8 and eq[1.0]["ratio_ceiling_from_link"] == 8.8e9 / 5e8
+    # 2 ms: the undrained 80k point does not count
+    assert eq[2.0]["batched_rate_per_s"] == 70e3 and eq[2.0]["ratio"] == 7e9 / 5e8
+    # 0.5 ms: the plain loop meets it at no rate -- null ratio and a note
+    assert eq[0.5]["ratio"] is None and eq[0.5]["ratio_ceiling_from_link"] is None
+    assert "every swept rate" in eq[0.5]["plain_note"] and "0.70 ms" in eq[0.5]["plain_note"]
+    assert "batched_note" not in eq[0.5]
