@@ -1030,7 +1030,8 @@ def swaptions_record(args, local, nsw=None, trials=None, steps=None, warmup=None
     g_s, _ = ctx.price_swaptions(sw, sample)
     ctx.close()
     threads = os.cpu_count() or 1
-    c_s, _, c_secs = oracle.swaptions_all(sw, sample, threads)
+    c_s, _, _ = oracle.swaptions_all(sw, sample, threads)  # the checker's build
+    _, _, c_secs = oracle.swaptions_all(sw, sample, threads, parsec_flags=True)  # timed
     rel = float(np.max(np.abs(g_s - c_s) / np.maximum(np.abs(c_s), 1e-12)))
     return {
         "workload": f"{nsw} swaptions x {trials} paths, 11-point HJM grid, 3 factors, one "
@@ -1041,7 +1042,7 @@ def swaptions_record(args, local, nsw=None, trials=None, steps=None, warmup=None
         "step_time_s": {"median": secs, "min": min(times), "max": max(times)},
         "prices": {"first": price[:4].tolist(), "std_err_first": err[:4].tolist()},
         "gpu_launches": launches,
-        "bound": "fp64 issue (the kernel reads no bulk data; ncu: FP64 pipe at ~87 % of peak)",
+        "bound": "fp64 issue (the kernel reads no bulk data; ncu: FP64 pipe at ~85 % of peak)",
         "vs_oracle": {"sample_trials": sample, "max_rel_price_diff": rel,
                       "note": "the same paths on the CPU oracle; parity with the reference "
                               "itself is unpinned (its model core is not in its tree)"},

@@ -218,12 +218,15 @@ def _parsec_lib() -> ctypes.CDLL:
     global _parsec
     if _parsec is None:
         so = os.path.join(HERE, "libbsoracle_parsec.so")
-        if not os.path.exists(so) or os.path.getmtime(so) < os.path.getmtime(
-                os.path.join(HERE, "bs_oracle.c")):
+        if not os.path.exists(so) or os.path.getmtime(so) < max(
+                os.path.getmtime(os.path.join(HERE, f)) for f in ("bs_oracle.c", "swpt_oracle.c")):
             build(ref=False)
         L = ctypes.CDLL(so)
         L.bso_bs_map.restype = ctypes.c_double
         L.bso_bs_map.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_size_t] + [_P] * 7
+        L.swo_price_all.restype = ctypes.c_double
+        L.swo_price_all.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64,
+                                    ctypes.c_int, _P, _P]
         _parsec = L
     return _parsec
 
@@ -294,14 +297,17 @@ def swaption_price(swaption, trials: int, unfloored: bool = False):
     return out[0], out[1]
 
 
-def swaptions_all(swaptions, trials: int, nthreads: int):
+def swaptions_all(swaptions, trials: int, nthreads: int, parsec_flags: bool = False):
     """Every swaption on nthreads threads (static partition, as the reference's
-    ParallelFor); returns (prices, standard errors, wall seconds)."""
+    ParallelFor); returns (prices, standard errors, wall seconds).
+    parsec_flags: the build with PARSEC's compiler flags (the timed baseline)."""
     arr, keep = _swo_structs(swaptions)
     n = len(swaptions)
     price = np.empty(n)
     err = np.empty(n)
-    secs = _swo_lib().swo_price_all(arr, n, trials, nthreads, _p(price), _p(err))
+    L = _parsec_lib() if parsec_flags else _swo_lib()
+    secs = L.swo_price_all(ctypes.cast(arr, ctypes.c_void_p) if parsec_flags else arr, n, trials,
+                           nthreads, _p(price), _p(err))
     if secs < 0:
         raise ValueError("swaption parameters out of the reference's range")
     return price, err, secs
