@@ -90,6 +90,30 @@ def test_each_result_same_alone_and_in_mix(gpu_ctx, kind):
         assert np.array_equal(alone[o:o + n].view(np.uint32), mix[o:o + n].view(np.uint32))
 
 
+@pytest.mark.parametrize("mode", ["sfu_ref", "libm_ref"])
+@pytest.mark.parametrize("kind", list(KINDS))
+def test_reference_order_modes_serve_the_maps_bits(gpu_ctx, kind, mode):
+    """The serving kernels in the reference-order modes: a mix of requests
+    (heads and tails off the vector grid, one option to 3 tiles) priced as
+    the map prices the same options in the same mode, bit for bit."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(17)
+    pool_n = 1 << 18
+    book, host = pinned_book(torch, pool_n, 43)
+    out = pinned_zeros(torch, pool_n)
+    reqs = disjoint_requests(rng, pool_n, 60, 6000)
+    with Server(budget_bytes=64 << 20, max_inflight=4, mode=mode, **KINDS[kind]) as srv:
+        for a in host + [out]:
+            srv.register(a)
+        ids = [srv.submit(*[a[o:] for a in host], out[o:], n=n) for o, n in reqs]
+        for rid in ids:
+            st, _ = srv.wait(rid, timeout_s=60.0)
+            assert st == OK
+    ref = gpu_ctx.price_book(book, mode=mode)
+    for i, (o, n) in enumerate(reqs):
+        assert np.array_equal(out[o:o + n].view(np.uint32), ref[o:o + n].view(np.uint32)), i
+
+
 def test_plain_mode_same_bits(gpu_ctx):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(6)
