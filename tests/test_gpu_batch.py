@@ -23,8 +23,9 @@ def layout(sizes, rng, gap_max=37):
     return segs, off
 
 
-@pytest.mark.parametrize("seed", [0, 1, 2])
-def test_batch_equals_per_book_and_plain(gpu_ctx, seed):
+@pytest.mark.parametrize("seed,mode", [(0, "fast"), (1, "fast"), (2, "fast"), (3, "sfu_ref"),
+                                       (4, "libm_ref")])
+def test_batch_equals_per_book_and_plain(gpu_ctx, seed, mode):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(seed)
     sizes = np.exp(rng.uniform(0, np.log(1 << 16), 300)).astype(np.int64)
@@ -36,12 +37,12 @@ def test_batch_equals_per_book_and_plain(gpu_ctx, seed):
     out_b = torch.full((pool_len,), -1.0, device="cuda:0")
     out_p = torch.full((pool_len,), -1.0, device="cuda:0")
     torch.cuda.synchronize()  # torch's copies and fills are done before the context's stream runs
-    gpu_ctx.price_batch(pool[:6], out_b, pool_len, segs, num_runs=1)
-    gpu_ctx.price_batch(pool[:6], out_p, pool_len, segs, num_runs=1, plain=True)
+    gpu_ctx.price_batch(pool[:6], out_b, pool_len, segs, num_runs=1, mode=mode)
+    gpu_ctx.price_batch(pool[:6], out_p, pool_len, segs, num_runs=1, plain=True, mode=mode)
     torch.cuda.synchronize()
     b = out_b.cpu().numpy()
     p = out_p.cpu().numpy()
-    whole = gpu_ctx.price_book(book)
+    whole = gpu_ctx.price_book(book, mode=mode)
     covered = np.zeros(pool_len, dtype=bool)
     for o, l in segs:
         covered[o:o + l] = True
