@@ -193,7 +193,9 @@ int bsg_price_books_plain(bsg_ctx* ctx, const float* sptprice, const float* stri
  *    cudaStream_t, NULL = legacy default stream).  Pool arrays are device
  *    memory, 16-byte aligned; segs is a host array.  flags: BSG_DEVICE_PTRS
  *    is implied; BSG_ASYNC returns once enqueued (keep segs alive until the
- *    stream reaches the call when it is pinned memory).
+ *    stream reaches the call when it is pinned memory).  It prices in the
+ *    fast mode only: any other flag, BSG_MODE_SFU_REF and BSG_MODE_LIBM_REF
+ *    included, is BSG_ERR_INVALID_ARG (checked before any CUDA call).
  *  - The first call on a device looks up the scratch array's device address
  *    (cudaGetSymbolAddress); make that first call before any stream capture.
  *    The address is kept per device together with the driver context it was

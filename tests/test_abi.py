@@ -56,3 +56,16 @@ def test_library_does_not_link_the_oracle():
     so = os.path.join(ROOT, "p3arsec_gb300", "libbsgpu.so")
     data = open(so, "rb").read()
     assert b"libbsoracle" not in data and b"bso_price" not in data
+
+
+def test_noalloc_refuses_reference_order_modes_before_any_cuda_call(lib):
+    """bsg_price_batch_noalloc prices in the fast mode only; a mode flag is
+    refused by the argument check, which runs before any CUDA call (so this
+    holds on a machine without a GPU)."""
+    from p3arsec_gb300 import abi
+    seg = (abi.Segment * 1)()
+    seg[0].offset, seg[0].len = 0, 1
+    for mode in ("sfu_ref", "libm_ref"):
+        st = lib.bsg_price_batch_noalloc(None, None, None, None, None, None, None, 1, seg, 1,
+                                         None, abi.MODES[mode])
+        assert st == -1  # BSG_ERR_INVALID_ARG
