@@ -118,3 +118,19 @@ def test_invalid_swaptions_are_refused(gpu_ctx):
     # the context still prices afterwards
     p, _ = gpu_ctx.price_swaptions(good, 1000)
     assert np.all(np.isfinite(p))
+
+
+def test_the_most_swaptions_one_call_takes(gpu_ctx, oracle_lib):
+    """65,535 swaptions (the grid's y extent) in one call at the fewest
+    trials (2), a few of them checked against the oracle; one more is
+    refused with BSG_ERR_CAPACITY before anything runs."""
+    from p3arsec_gb300.abi import BsgError
+    sw = S.generate(65535, seed=8)
+    got, err = gpu_ctx.price_swaptions(sw, 2)
+    assert got.shape == (65535,) and np.all(np.isfinite(got)) and np.all(np.isfinite(err))
+    for i in (0, 1, 32767, 65534):
+        p, e = oracle_lib.swaption_price(sw[i], 2)
+        check(got[i:i + 1], err[i:i + 1], np.array([p]), np.array([e]))
+    with pytest.raises(BsgError) as e:
+        gpu_ctx.price_swaptions(sw + sw[:1], 2)
+    assert e.value.status == -5  # BSG_ERR_CAPACITY
