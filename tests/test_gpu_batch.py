@@ -133,3 +133,25 @@ def test_batch_autotune_and_every_shape_gives_the_same_bits(gpu_ctx):
                     assert np.array_equal(got[o:o + l].view(np.uint32), ref[o:o + l].view(np.uint32))
     finally:
         gpu_ctx.set_batch_tune(**saved)
+
+
+def test_batch_of_many_tiny_books(gpu_ctx):
+    """100,000 books of 0 to 9 options (most shorter than one vector group,
+    every start unaligned): one tile each, all priced as the map prices
+    them, gaps untouched."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(29)
+    segs, pool_len = layout(rng.integers(0, 10, 100_000), rng, gap_max=5)
+    book = books.generate(pool_len, seed=31)
+    pool = pool_on_device(torch, book)
+    out = torch.full((pool_len,), -1.0, device="cuda:0")
+    torch.cuda.synchronize()  # torch's copies and fills are done before the context's stream runs
+    gpu_ctx.price_batch(pool, out, pool_len, segs, num_runs=3)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    whole = gpu_ctx.price_book(book)
+    covered = np.zeros(pool_len, dtype=bool)
+    for o, l in segs:
+        covered[o:o + l] = True
+    assert np.array_equal(got[covered].view(np.uint32), whole[covered].view(np.uint32))
+    assert np.all(got[~covered] == -1.0)
