@@ -305,7 +305,8 @@ void bsg_server_destroy(bsg_server* srv);
  * array of a batched request must lie inside one registered range: the GPU
  * reads inputs and writes prices there directly over the host link. */
 int bsg_server_register(bsg_server* srv, void* ptr, size_t bytes);
-/* Enqueues a request (non-blocking).  BSG_ERR_BUDGET if it can never fit. */
+/* Enqueues a request (non-blocking).  BSG_ERR_BUDGET if it can never fit.
+ * A request of n == 0 options completes at once with BSG_OK. */
 int bsg_server_submit(bsg_server* srv, const bsg_request* req, uint64_t* id);
 /* Waits up to timeout_s (< 0: no limit) for request id.  Returns its final
  * status (BSG_OK priced, BSG_ERR_CANCELLED, BSG_ERR_TIMEOUT for a batch that

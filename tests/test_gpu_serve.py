@@ -114,6 +114,27 @@ def test_reference_order_modes_serve_the_maps_bits(gpu_ctx, kind, mode):
         assert np.array_equal(out[o:o + n].view(np.uint32), ref[o:o + n].view(np.uint32)), i
 
 
+@pytest.mark.parametrize("kind", list(KINDS))
+def test_empty_requests_complete_at_once_among_others(gpu_ctx, kind):
+    torch = pytest.importorskip("torch")
+    book, host = pinned_book(torch, 1 << 16, 47)
+    out = pinned_zeros(torch, 1 << 16)
+    with Server(budget_bytes=64 << 20, max_inflight=4, **KINDS[kind]) as srv:
+        for a in host + [out]:
+            srv.register(a)
+        ids = []
+        for i, (o, n) in enumerate([(0, 0), (100, 5000), (9000, 0), (20000, 3), (30000, 0)]):
+            ids.append((o, n, srv.submit(*[a[o:] for a in host], out[o:], n=n)))
+        for o, n, rid in ids:
+            st, _ = srv.wait(rid, timeout_s=60.0)
+            assert st == OK, (o, n)
+        assert srv.stats()["completed"] == 5
+    ref = gpu_ctx.price_book(book)
+    for o, n, _ in ids:
+        assert np.array_equal(out[o:o + n].view(np.uint32), ref[o:o + n].view(np.uint32))
+    assert out[9000] == 0.0 and out[30000] == 0.0  # the empty requests wrote nothing
+
+
 def test_plain_mode_same_bits(gpu_ctx):
     torch = pytest.importorskip("torch")
     rng = np.random.default_rng(6)
