@@ -683,7 +683,8 @@ def serve_point(host, out, mode, rate, seconds, args, local, seed, sizes=None):
                            drain_timeout_s=60.0,
                            fused=(mode == "batched" and args.serve_fused >= 1),
                            persistent=(mode == "batched" and args.serve_fused == 2),
-                           persistent_blocks=args.serve_blocks)
+                           persistent_blocks=args.serve_blocks,
+                           persistent_window=args.serve_window)
 
 
 def equal_p99(sweep, bounds_ms, link_opts):
@@ -1195,6 +1196,8 @@ def main(argv=None):
                          "0: gather, price, scatter")
     ap.add_argument("--serve-blocks", type=int, default=0,
                     help="serve: blocks of the persistent kernel (0 = SMs x min(occupancy, 3))")
+    ap.add_argument("--serve-window", type=int, default=0,
+                    help="serve: requests the persistent kernel's blocks share (0 = default)")
     ap.add_argument("--serve-block-list", default="16,32,64,128,0",
                     help="serve-blocks config: the persistent kernel's grid sizes to sweep")
     ap.add_argument("--serve-block-rates", default="20000,60000,70000,80000",

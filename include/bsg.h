@@ -275,6 +275,9 @@ typedef struct bsg_server_config {
                                  0 = gather into the pool, price, scatter */
     int persistent_blocks;    /* fused = 2: blocks of the persistent kernel,
                                  8..4096 (0 = SMs x min(occupancy, 3)) */
+    int persistent_window;    /* fused = 2: how many of the oldest requests
+                                 the blocks share at once, 1..16 (0 = the
+                                 default; 1 = the oldest request's tiles first) */
 } bsg_server_config;
 
 typedef struct bsg_request {

@@ -69,7 +69,8 @@ class ServerConfig(ctypes.Structure):
                 ("max_inflight", ctypes.c_int), ("max_batch_options", ctypes.c_size_t),
                 ("max_batch_requests", ctypes.c_int), ("plain", ctypes.c_int),
                 ("flags", ctypes.c_uint), ("batch_timeout_s", ctypes.c_double),
-                ("fused", ctypes.c_int), ("persistent_blocks", ctypes.c_int)]
+                ("fused", ctypes.c_int), ("persistent_blocks", ctypes.c_int),
+                ("persistent_window", ctypes.c_int)]
 
 
 class Request(ctypes.Structure):
@@ -461,12 +462,12 @@ class Server:
 
     def __init__(self, device=0, budget_bytes=64 << 30, max_inflight=4, max_batch_options=0,
                  max_batch_requests=0, plain=False, mode="fast", batch_timeout_s=30.0,
-                 fused=True, persistent=False, persistent_blocks=0):
+                 fused=True, persistent=False, persistent_blocks=0, persistent_window=0):
         self.lib = load()
         self.cfg = ServerConfig(device, budget_bytes, max_inflight, max_batch_options,
                                 max_batch_requests, 1 if plain else 0, MODES[mode],
                                 batch_timeout_s, 2 if persistent else (1 if fused else 0),
-                                persistent_blocks)
+                                persistent_blocks, persistent_window)
         h = _P()
         st = self.lib.bsg_server_create(ctypes.byref(h), ctypes.byref(self.cfg))
         if st != 0:
@@ -522,12 +523,14 @@ class Server:
 def serve_trace(host_pool, prices, rate_per_s, duration_s, min_n=16, max_n=1 << 20, seed=1,
                 device=0, budget_bytes=64 << 30, max_inflight=4, plain=False, mode="fast",
                 max_batch_options=0, max_batch_requests=0, drain_timeout_s=60.0,
-                latencies=None, fused=True, persistent=False, persistent_blocks=0):
+                latencies=None, fused=True, persistent=False, persistent_blocks=0,
+                persistent_window=0):
     """bsg_serve_trace over a host pool (6 arrays) and a prices array."""
     lib = load()
     cfg = ServerConfig(device, budget_bytes, max_inflight, max_batch_options, max_batch_requests,
                        1 if plain else 0, MODES[mode], 30.0,
-                       2 if persistent else (1 if fused else 0), persistent_blocks)
+                       2 if persistent else (1 if fused else 0), persistent_blocks,
+                       persistent_window)
     n = len(host_pool[0])
     tc = TraceConfig(rate_per_s, duration_s, min_n, max_n, seed, *[ptr(a) for a in host_pool],
                      ptr(prices), n, drain_timeout_s)

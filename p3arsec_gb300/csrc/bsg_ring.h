@@ -7,7 +7,9 @@
 //
 //   claim word = tag (low 32 bits of r) << 32 | ntiles << 20 | tiles claimed
 //
-// A worker that is about to work on request r (already published):
+// A worker that is about to work on request r (already published; any
+// published request, not only the oldest: claim_window spreads the workers
+// over the oldest few):
 //   * finds the slot tagged with an earlier lap: it re-arms the word for r
 //     (CAS from the value it saw to tag r, ntiles of r, count 0);
 //   * finds tag r: one fetch-add claims the tile numbered by the count it
@@ -75,6 +77,10 @@ BSG_RING_FN int claim(Ops& ops, uint64_t r, uint64_t rmask, uint64_t* req, uint6
             continue;
         }
         if (lap > 0) return kFinished;  // a later lap: r is done
+        // every tile of r already claimed (counts only grow within a lap):
+        // no add, so that repeated attempts on a finished request do not
+        // run its count up
+        if (count_of(w) >= ntiles_of(w)) return kFinished;
         const uint64_t old = ops.add(slot);
         const int lap_old = (int)(tag_of(old) - tag);
         if (count_of(old) < ntiles_of(old) && lap_old >= 0) {
@@ -91,6 +97,40 @@ BSG_RING_FN int claim(Ops& ops, uint64_t r, uint64_t rmask, uint64_t* req, uint6
         }
         return kFinished;  // every tile of r is claimed
     }
+}
+
+// True when claim word w (of request r's slot) shows no unclaimed tile of r.
+BSG_RING_FN bool word_exhausted(uint64_t w, uint64_t r) {
+    const int lap = (int)(tag_of(w) - (uint32_t)r);
+    return lap > 0 || (lap == 0 && count_of(w) >= ntiles_of(w));
+}
+
+// True when published request r has no unclaimed tile left (one load; a
+// slot not yet armed for r counts as not exhausted).
+#if defined(__CUDACC__)
+#pragma nv_exec_check_disable
+#endif
+template <class Ops>
+BSG_RING_FN bool exhausted(Ops& ops, uint64_t r, uint64_t rmask) {
+    return word_exhausted(ops.load(r & rmask), r);
+}
+
+// One attempt to claim a tile of one of the oldest published requests
+// [r0, r0 + min(pub - r0, window)), trying them in turn from r0 + start
+// (mod the window's size): requests in flight share the workers instead of
+// waiting for the oldest to be fully claimed.  kTile as claim() reports it,
+// or kFinished when no request of the window has an unclaimed tile.
+// window <= ring size, r0 < pub.
+#if defined(__CUDACC__)
+#pragma nv_exec_check_disable
+#endif
+template <class Ops>
+BSG_RING_FN int claim_window(Ops& ops, uint64_t r0, uint64_t pub, uint64_t rmask, uint64_t window,
+                             uint64_t start, uint64_t* req, uint64_t* tile, uint64_t* ntiles) {
+    const uint64_t w = (pub - r0 < window) ? pub - r0 : window;
+    for (uint64_t k = 0; k < w; ++k)
+        if (claim(ops, r0 + (start + k) % w, rmask, req, tile, ntiles) == kTile) return kTile;
+    return kFinished;
 }
 
 // Counts one priced tile of the request in `slot` (ntiles tiles); true for

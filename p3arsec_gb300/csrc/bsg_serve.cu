@@ -301,6 +301,11 @@ cudaError_t launch_fused_inline(int mode, unsigned grid, cudaStream_t st, const 
 // flag), after which the block exits; the host relaunches the kernel when
 // work arrives and no kernel is running.
 constexpr uint64_t kMaxRequestTiles = bsg_ring::kMaxTiles;  // 12 bits of the claim word
+// Requests the persistent kernel's blocks share at once (bsg_ring::claim_window);
+// 1 = the oldest request's tiles first.
+constexpr unsigned long long kDefaultWindow = 1;
+constexpr unsigned long long kMaxWindow = 16;  // claim words a block loads at once
+constexpr int kDescCache = 4;                  // request descriptors a block keeps
 
 struct alignas(128) PEntry {
     unsigned long long flag;    // seq + 1 once every tile is priced (GPU writes)
@@ -369,10 +374,15 @@ struct DeviceRingOps {
 template <int M>
 __global__ void __launch_bounds__(kThreads) serve_persistent_kernel(
     PEntry* ring, unsigned long long rmask, const PCtl* ctl, unsigned long long* cur,
-    unsigned long long* taken, unsigned* done, unsigned long long idle_ns) {
+    unsigned long long* taken, unsigned* done, unsigned long long idle_ns,
+    unsigned long long window) {
     __shared__ Desc sh_d;
     __shared__ unsigned long long sh_b, sh_seq, sh_nt;
     __shared__ int sh_ok;
+    __shared__ Desc sh_cache[kDescCache];
+    __shared__ unsigned long long sh_cseq[kDescCache];
+    if (threadIdx.x < kDescCache) sh_cseq[threadIdx.x] = ~0ull;
+    __syncthreads();
     // thread 0's view of `published` (re-read from host memory only when the
     // ring looks drained) and the request whose descriptor sh_d holds.  While
     // idle, only the first kScouts blocks poll host memory; they copy what
@@ -382,7 +392,7 @@ __global__ void __launch_bounds__(kThreads) serve_persistent_kernel(
     constexpr unsigned kScouts = 8;
     const bool scout = blockIdx.x < kScouts;
     unsigned long long* pub_dev = cur + 1;
-    unsigned long long pub = 0, d_seq = ~0ull;
+    unsigned long long pub = 0, d_seq = ~0ull, rot = 0, cnext = 0;
     for (;;) {
         if (threadIdx.x == 0) {
             sh_ok = 0;
@@ -408,7 +418,39 @@ __global__ void __launch_bounds__(kThreads) serve_persistent_kernel(
                 }
                 DeviceRingOps ops{taken, done, ring};
                 uint64_t q = 0, c = 0, nt = 0;
-                if (bsg_ring::claim(ops, r, rmask, &q, &c, &nt) == bsg_ring::kTile) {
+                int got = bsg_ring::kFinished;
+                if (window <= 1) {
+                    // the oldest request's tiles first, in order of arrival
+                    got = bsg_ring::claim(ops, r, rmask, &q, &c, &nt);
+                } else {
+                    // a tile of one of the w oldest published requests, so
+                    // that requests in flight share the blocks: their claim
+                    // words loaded together (one round trip), the cursor
+                    // moved past the leading finished ones, then the live
+                    // ones tried from this block's rotating offset (each
+                    // claim as bsg_ring::claim_window makes it)
+                    const uint64_t w = (pub - r < window) ? pub - r : window;
+                    uint64_t wv[kMaxWindow];
+#pragma unroll
+                    for (int k = 0; k < (int)kMaxWindow; ++k)
+                        if ((uint64_t)k < w) wv[k] = ops.load((r + k) & rmask);
+                    uint64_t lead = 0;
+                    while (lead < w && bsg_ring::word_exhausted(wv[lead], r + lead)) ++lead;
+                    if (lead > 0) {
+                        atomicCAS(cur, r, r + lead);
+                        if (lead == w) {
+                            t0 = global_ns();
+                            backoff = 64;
+                            continue;
+                        }
+                    }
+                    uint64_t i = (blockIdx.x + rot++) % w;
+                    for (uint64_t k = 0; k < w && got != bsg_ring::kTile; ++k, i = (i + 1 == w) ? 0 : i + 1)
+                        if (!bsg_ring::word_exhausted(wv[i], r + i))
+                            got = bsg_ring::claim(ops, r + i, rmask, &q, &c, &nt);
+                    if (got != bsg_ring::kTile) continue;  // claimed meanwhile: look again
+                }
+                if (got == bsg_ring::kTile) {
                     // a tile of q: r, or a later request of the same slot,
                     // which another block armed after seeing it published;
                     // see that publication here too before reading q's entry
@@ -416,8 +458,20 @@ __global__ void __launch_bounds__(kThreads) serve_persistent_kernel(
                     for (int i = 0; q >= pub && i < (1 << 20); ++i)
                         pub = ld_acquire_sys(&ctl->published);
                     const unsigned long long slot = q & rmask;
-                    if (d_seq != q) {  // consecutive tiles of one request: read once
-                        sh_d = ring[slot].d;
+                    if (d_seq != q) {
+                        // the descriptors of the last kDescCache requests
+                        // this block priced stay in shared memory: a block
+                        // moving between requests reads each from host
+                        // memory once
+                        int hit = -1;
+                        for (int k = 0; k < kDescCache; ++k)
+                            if (sh_cseq[k] == q) hit = k;
+                        if (hit < 0) {
+                            hit = (int)(cnext++ % kDescCache);
+                            sh_cache[hit] = ring[slot].d;
+                            sh_cseq[hit] = q;
+                        }
+                        sh_d = sh_cache[hit];
                         d_seq = q;
                     }
                     sh_b = c * kTile;
@@ -426,7 +480,7 @@ __global__ void __launch_bounds__(kThreads) serve_persistent_kernel(
                     sh_ok = 1;
                     break;
                 }
-                atomicCAS(cur, r, r + 1);  // r has no unclaimed tile: move on
+                atomicCAS(cur, r, r + 1);  // r (the window) has no unclaimed tile: move on
                 t0 = global_ns();
                 backoff = 64;
             }
@@ -450,16 +504,16 @@ __global__ void __launch_bounds__(kThreads) serve_persistent_kernel(
 cudaError_t launch_persistent(int mode, unsigned grid, cudaStream_t st, PEntry* ring,
                               unsigned long long rmask, const PCtl* ctl, unsigned long long* cur,
                               unsigned long long* taken, unsigned* done,
-                              unsigned long long idle_ns) {
+                              unsigned long long idle_ns, unsigned long long window) {
     switch (mode) {
         case bsg::MODE_FAST:
-            serve_persistent_kernel<bsg::MODE_FAST><<<grid, kThreads, 0, st>>>(ring, rmask, ctl, cur, taken, done, idle_ns);
+            serve_persistent_kernel<bsg::MODE_FAST><<<grid, kThreads, 0, st>>>(ring, rmask, ctl, cur, taken, done, idle_ns, window);
             break;
         case bsg::MODE_SFU_REF:
-            serve_persistent_kernel<bsg::MODE_SFU_REF><<<grid, kThreads, 0, st>>>(ring, rmask, ctl, cur, taken, done, idle_ns);
+            serve_persistent_kernel<bsg::MODE_SFU_REF><<<grid, kThreads, 0, st>>>(ring, rmask, ctl, cur, taken, done, idle_ns, window);
             break;
         default:
-            serve_persistent_kernel<bsg::MODE_LIBM_REF><<<grid, kThreads, 0, st>>>(ring, rmask, ctl, cur, taken, done, idle_ns);
+            serve_persistent_kernel<bsg::MODE_LIBM_REF><<<grid, kThreads, 0, st>>>(ring, rmask, ctl, cur, taken, done, idle_ns, window);
             break;
     }
     return cudaGetLastError();
@@ -556,6 +610,7 @@ struct bsg_server {
     cudaStream_t pst = nullptr;
     cudaEvent_t pev = nullptr;            // recorded after each launch of the kernel
     unsigned pgrid = 1;
+    unsigned long long pwindow = 1;       // requests the blocks share (claim_window)
     uint64_t next_seq = 0;
     std::deque<Request*> pinflight;       // published, not complete, in sequence order
     uint64_t cap = 0;  // options
@@ -745,7 +800,8 @@ struct bsg_server {
         cudaGetDevice(&prev);
         if (prev != device) cudaSetDevice(device);
         const bool ok = launch_persistent(mode, pgrid, pst, ring_d, kRing - 1, ctl_d, d_cur,
-                                          d_taken, d_done, kIdleNs) == cudaSuccess &&
+                                          d_taken, d_done, kIdleNs,
+                                          std::min<unsigned long long>(pwindow, kMaxWindow)) == cudaSuccess &&
                         cudaEventRecord(pev, pst) == cudaSuccess;
         if (prev != device) cudaSetDevice(prev);
         if (!ok) {
@@ -1168,7 +1224,8 @@ int bsg_server_create(bsg_server** out, const bsg_server_config* cfg) {
     *out = nullptr;
     if (cfg->max_inflight < 1 || cfg->max_inflight > 16 || cfg->max_batch_requests < 0 ||
         cfg->max_batch_requests > 65536 || cfg->budget_bytes < 28 * kAlign ||
-        (cfg->persistent_blocks != 0 && (cfg->persistent_blocks < 8 || cfg->persistent_blocks > 4096)))
+        (cfg->persistent_blocks != 0 && (cfg->persistent_blocks < 8 || cfg->persistent_blocks > 4096)) ||
+        cfg->persistent_window < 0 || cfg->persistent_window > (int)kMaxWindow)
         return BSG_ERR_INVALID_ARG;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || cfg->device < 0 || cfg->device >= ndev) {
@@ -1245,6 +1302,8 @@ int bsg_server_create(bsg_server** out, const bsg_server_config* cfg) {
             // on a loaded link, so the link needs ~40+ blocks; 3 per SM
             s->pgrid = cfg->persistent_blocks ? (unsigned)cfg->persistent_blocks
                                               : (unsigned)(s->sm_count * std::min(occ, 3));
+            s->pwindow = cfg->persistent_window ? (unsigned long long)cfg->persistent_window
+                                                : kDefaultWindow;
             break;  // no device pool and no batch slots on this path
         }
         // the device pool holds requests only on the unfused and plain paths;

@@ -6,7 +6,11 @@
 // completion is reported exactly once per request and only after all its
 // tiles were done, and that nothing is left unclaimed.
 //
-//   ring_model_check <requests> <workers> <ring> <seed>   -> prints "ok"
+//   ring_model_check <requests> <workers> <ring> <seed> [window]   -> prints "ok"
+//
+// window 1 (the default): every worker claims from the oldest request with
+// unclaimed tiles; window W > 1: from the W oldest published requests, each
+// worker starting at its own rotating offset (claim_window).
 #include <atomic>
 #include <cstdio>
 #include <cstdlib>
@@ -42,11 +46,13 @@ int fail(const char* what, uint64_t a, uint64_t b) {
 }  // namespace
 
 int main(int argc, char** argv) {
-    if (argc != 5) return fail("usage", 0, 0);
+    if (argc != 5 && argc != 6) return fail("usage", 0, 0);
+    const uint64_t window = argc == 6 ? std::strtoull(argv[5], nullptr, 10) : 1;
     const uint64_t nreq = std::strtoull(argv[1], nullptr, 10);
     const int nworkers = std::atoi(argv[2]);
     const uint64_t ring = std::strtoull(argv[3], nullptr, 10);  // a power of two
     const uint64_t rmask = ring - 1;
+    if (window < 1 || window > ring) return fail("window must be 1..ring", window, ring);
     std::mt19937_64 rng(std::strtoull(argv[4], nullptr, 10));
     std::vector<uint64_t> ntiles(nreq), first(nreq + 1, 0);
     for (uint64_t r = 0; r < nreq; ++r) {
@@ -82,22 +88,34 @@ int main(int argc, char** argv) {
         workers.emplace_back([&, w] {
             HostOps ops{taken.data(), done.data(), nt.data()};
             std::mt19937 jitter(w);
+            uint64_t rot = 0;
             while (completed.load(std::memory_order_acquire) < nreq) {
                 const uint64_t r = cur.load(std::memory_order_relaxed);
                 if (jitter() % 8 == 0) std::this_thread::yield();  // stale views of cur
-                if (r >= published.load(std::memory_order_acquire)) {
+                const uint64_t pub = published.load(std::memory_order_acquire);
+                if (r >= pub) {
                     std::this_thread::yield();
                     continue;
                 }
                 uint64_t q = 0, tile = 0, n = 0;
-                if (bsg_ring::claim(ops, r, rmask, &q, &tile, &n) != bsg_ring::kTile) {
+                int got;
+                if (window == 1) {
+                    got = bsg_ring::claim(ops, r, rmask, &q, &tile, &n);
+                } else if (bsg_ring::exhausted(ops, r, rmask)) {
+                    got = bsg_ring::kFinished;
+                } else {
+                    got = bsg_ring::claim_window(ops, r, pub, rmask, window, (uint64_t)w + rot++, &q,
+                                                 &tile, &n);
+                }
+                if (got != bsg_ring::kTile) {
                     uint64_t e = r;
                     cur.compare_exchange_strong(e, r + 1, std::memory_order_acq_rel);
                     continue;
                 }
-                // q is r or a later request of the same slot, already published
-                if (q < r || (q - r) % ring != 0 || q >= published.load(std::memory_order_acquire))
-                    bad = 5;
+                // q is a request of the window (or a later request of one of
+                // its slots), already published
+                if (q < r || q >= published.load(std::memory_order_acquire)) bad = 5;
+                if (window == 1 && (q - r) % ring != 0) bad = 5;
                 if (q >= nreq || n != ntiles[q] || tile >= n) {
                     bad = 1;
                     continue;

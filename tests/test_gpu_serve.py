@@ -14,7 +14,9 @@ pytestmark = pytest.mark.gpu
 
 OK, TIMEOUT, CANCELLED, BUDGET, CAPACITY, STATE = 0, -7, -9, -8, -5, -11
 KINDS = {"unfused": dict(fused=False), "fused": dict(fused=True),
-         "persistent": dict(persistent=True)}
+         "persistent": dict(persistent=True),
+         # the persistent kernel's blocks shared by the 16 oldest requests
+         "persistent_w16": dict(persistent=True, persistent_window=16)}
 
 
 def pinned_book(torch, n, seed):
@@ -70,7 +72,7 @@ def test_each_result_same_alone_and_in_mix(gpu_ctx, kind):
             assert st == OK and lat > 0
         stats = srv.stats()
         assert stats["completed"] == len(reqs)
-        if kind == "persistent":
+        if kind.startswith("persistent"):
             # every request went to the one running kernel (relaunched at
             # most after an idle exit), none needed a launch of its own
             assert stats["kernel_launches"] <= 3

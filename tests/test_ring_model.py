@@ -42,3 +42,20 @@ def test_claim_protocol_two_slots_many_workers(model, seed):
     r = subprocess.run([model, "600", "16", "2", str(seed)], stdout=subprocess.PIPE,
                        stderr=subprocess.STDOUT, text=True, timeout=300)
     assert r.returncode == 0 and r.stdout.startswith("ok"), r.stdout
+
+
+@pytest.mark.parametrize("requests,workers,ring,seed,window", [
+    (10000, 8, 8, 1, 8),    # the window as wide as the ring
+    (10000, 16, 4, 2, 2),
+    (3000, 16, 2, 3, 2),    # two slots: re-armed words under windowed claims
+    (20000, 12, 64, 4, 32),
+    (20000, 6, 4096, 5, 32),  # the kernel's ring and window
+])
+def test_windowed_claims_exactly_once(model, requests, workers, ring, seed, window):
+    """Workers spread over the oldest `window` published requests
+    (claim_window, starting at rotating offsets; the oldest advanced past
+    once exhausted): still every tile claimed exactly once and every request
+    completed once."""
+    r = subprocess.run([model, str(requests), str(workers), str(ring), str(seed), str(window)],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=300)
+    assert r.returncode == 0 and r.stdout.startswith("ok"), r.stdout
