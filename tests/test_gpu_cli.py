@@ -62,3 +62,24 @@ def test_swaptions_cli_prices_like_the_oracle():
     want, want_err, _ = oracle.swaptions_all(S.generate_cli(6, seed=7), 20000, 4)
     assert np.allclose(got[:, 0], want, rtol=1e-10, atol=1e-9)
     assert np.allclose(got[:, 1], want_err, rtol=1e-6, atol=1e-9)
+
+
+def test_cli_at_two_million_options(tmp_path):
+    """The drop-in at scale: a 2M-option PARSEC file (~150 MB, split across
+    the parser's threads) through the CLI with the reference's ERR_CHK
+    against FP64 DGrefval, and the printed prices against the FP64 oracle."""
+    build.build()
+    n = 1 << 21
+    book = books.generate(n, seed=37)
+    fp64 = oracle.price_fp64(book)
+    inp = tmp_path / "in.txt"
+    out = tmp_path / "out.txt"
+    books.write_parsec_input(inp, book, dgrefval=fp64)
+    env = dict(os.environ, BSG_ERR_CHK="1", BSG_NUM_RUNS="3")
+    r = subprocess.run([build.CLI, "16", str(inp), str(out)], stdout=subprocess.PIPE,
+                       stderr=subprocess.STDOUT, text=True, env=env, timeout=300)
+    assert r.returncode == 0, r.stdout
+    assert f"Num of Options: {n}" in r.stdout and "Num Errors: 0" in r.stdout
+    got = books.read_parsec_output(out)
+    assert got.shape == (n,)
+    assert np.abs(got.astype(np.float64) - fp64).max() <= 1e-4
